@@ -1,0 +1,298 @@
+#!/usr/bin/env python
+"""Throughput of the batched Monte Carlo trap kinetics (electron-steps/s).
+
+Workload (one "step" = one pass of the kinetics over the whole batch):
+4,096 parameter sets, E ~ U[1.2, 1.8] eV, log10 s ~ U[10, 14],
+rho' log-uniform [1e-7, 1e-5] (alpha = rho'^(-1/3)), 1e3..1e5 traps per set
+(log-uniform, ragged, 8.8e7 traps in all); even sets are TL ramps
+(beta in {0.5, 1, 2, 5} K/s, 0 -> 500 degC, dt = 0.1 s, 1 degC bins), odd sets
+isothermal holds (150..300 degC, 1e4 s, dt = 1 s, 20 s bins): 6.46e11
+electron-step trials per pass, FP32 with native Philox4x32-10 uniforms.
+
+``value``    trials / device time of one pass (CUDA events around the graph
+             replay on its stream; L2 flushed between passes).
+``e2e``      the same through the public API with host buffers:
+             simulate_batch(specs) packs, validates, uploads, launches and
+             reads the bins back every step.
+``--impl reference``  the CPU restatement of the kinetics (numpy, FP64) on
+             the host cores, over a bounded sample of the same sets.
+
+Multi-GPU (torchrun): every rank runs its own 4,096-set batch (weak scaling);
+sets are independent, so there is no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_SETS = 4096
+WORKLOAD = "batch_tl_iso"
+METRIC = "MC electron-steps/s"
+UNIT = "electron-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--seed", type=int, default=20261203)
+    p.add_argument("--block", type=int, default=0)
+    p.add_argument("--ept", type=int, default=0)
+    p.add_argument("--sets", type=int, default=N_SETS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="CPU work budget of the CPU-baseline sample")
+    return p.parse_args()
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ---------------------------------------------------------------------------
+# CPU port (the oracle restatement, timed as the baseline)
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    st, seed = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle import bernoulli as ob
+    t0 = time.perf_counter()
+    ob.run_set(st, layout="numpy", seed=seed)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(specs, budget_s):
+    """A deterministic sample of the sets whose trials fit ~budget_s of CPU
+    work at ~1e8 trials/s/core, spread over the whole batch."""
+    cores = os.cpu_count() or 1
+    target = budget_s * 1e8 * cores
+    order = list(range(0, len(specs), 7)) + [i for i in range(len(specs)) if i % 7]
+    pick, tot = [], 0
+    for i in order:
+        if tot >= target:
+            break
+        pick.append(i)
+        tot += specs[i].trials
+    return pick, tot
+
+
+def run_cpu(specs, pick, seed):
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    jobs = [(specs[i].to_dict(), seed) for i in sorted(pick, key=lambda i: -specs[i].trials)]
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        list(pool.imap_unordered(_cpu_worker, jobs))
+    wall = time.perf_counter() - t0
+    trials = sum(specs[i].trials for i in pick)
+    return trials / wall, wall, trials, cores
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(index)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except Exception:
+            self.p.kill()
+            out = ""
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    a = parse()
+    rank, world, local = env_rank()
+    if a.impl == "reference":
+        return main_reference(a, rank, world)
+    import torch
+    from mcluminescence_gb300 import BernoulliBatch, schedule, simulate_batch
+    from mcluminescence_gb300 import autotune
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    specs = schedule.batch_tl_iso(a.sets, seed=a.seed + 7919 * rank)
+    for s in specs:
+        s.set_id += rank * a.sets
+    block, ept = a.block, a.ept
+    if not block or not ept:
+        block, ept = autotune.pick_bernoulli(specs, precision="fp32")
+    batch = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=block, ept=ept,
+                           want_alive=True)
+    stream = torch.cuda.Stream()
+    batch.capture(stream)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    for _ in range(a.warmup):
+        batch.replay(stream)
+    stream.synchronize()
+    assert batch.status() == 0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = Clocks(torch.cuda.current_device())
+    barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(a.steps)]
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()                      # evict L2 between passes (untimed)
+        ev[k][0].record(stream)
+        batch.replay(stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    if batch.status() != 0:
+        raise RuntimeError(f"kernel status {batch.status()}")
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / a.steps
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+    trials = batch.trials
+    total_trials = trials * world
+    value = total_trials / (ms_max / 1e3)
+
+    # ---- end to end through the public API (host specs in, host bins out) ----
+    e2e = None
+    if not a.no_e2e:
+        res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / a.steps
+        if world > 1:
+            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = batch.host_sets.nbytes + batch.host_segs.nbytes + batch.host_items.nbytes
+        d2h = 4 * batch.n_bins_total * 2 + 4
+        e2e = {"value": total_trials / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+               "path": "mcluminescence_gb300.simulate_batch (host specs -> host bins)"}
+
+    # ---- roofline of the dominant kernel ------------------------------------
+    from mcluminescence_gb300 import roofline
+    roof = roofline.bernoulli_fp32(trials, ms / 1e3, clk.get("sm_mhz"))
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+u32(philox)",
+        "data": "synthetic (seeded parameter sets of the batched TL + isothermal shape)",
+        "config": {"workload": f"{WORKLOAD}: {a.sets} sets/GPU, ragged 1e3..1e5 traps, "
+                               "half TL ramps (0.5-5 K/s to 500 C, dt 0.1 s), half isothermal "
+                               "(150-300 C, 1e4 s, dt 1 s)",
+                   "sets_per_gpu": a.sets, "traps_per_gpu": int(sum(s.n_slots for s in specs)),
+                   "trials_per_step_per_gpu": int(trials), "precision": "fp32",
+                   "rng": "philox4x32-10", "block": block, "ept": ept, "n_items": batch.n_items,
+                   "l2": "flushed between passes (256 MB write, untimed)",
+                   "parallelism": f"replicas x{world} (independent sets, no collective)"},
+        "e2e": e2e, "gpu_launches": a.steps, "clocks": clk, "roofline": roof,
+        "wall_s_timed": t_wall,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        pick, _ = cpu_sample(specs, a.cpu_seconds)
+        v, wall, tr, cores = run_cpu(specs, pick, a.seed)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"{len(pick)} of the {a.sets} sets ({tr:.3e} trials, "
+                                         f"{wall:.1f} s wall), oracle FP64 numpy restatement, "
+                                         f"one process per core"}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def main_reference(a, rank, world):
+    """The CPU restatement of the kinetics (the reference has no compiled or GPU
+    path) on this host's cores, on a bounded sample of the same workload."""
+    if rank != 0:
+        return
+    from mcluminescence_gb300 import schedule
+    specs = schedule.batch_tl_iso(a.sets, seed=a.seed)
+    pick, _ = cpu_sample(specs, a.cpu_seconds)
+    times = []
+    for k in range(a.warmup + a.steps):
+        v, wall, tr, cores = run_cpu(specs, pick, a.seed + k)
+        if k >= a.warmup:
+            times.append(wall)
+    wall = statistics.mean(times)
+    value = tr / wall
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded parameter sets of the batched TL + isothermal shape)",
+        "config": {"workload": f"{WORKLOAD}: sample of {len(pick)} of {a.sets} sets",
+                   "trials_per_step": int(tr)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(pick)} sets, {tr:.3e} trials per step, oracle FP64 "
+                                   "numpy restatement, one process per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,166 @@
+/*
+ * mclum.h -- C ABI of the GB300 (sm_103a) Monte Carlo trap-kinetics library.
+ *
+ * Plain C: pointers, sizes and POD structs only; no CUDA or torch types.
+ * Device pointers are caller-owned (e.g. torch tensors); streams are passed as
+ * `void*` holding a cudaStream_t (NULL = the legacy default stream).  Every
+ * entry point returns MCL_OK (0) or a negative MCL_E* code; kernels report
+ * problems they detect on the device through a caller-provided int32 status
+ * word (0 = fine), never by trapping.
+ *
+ * The reference is a Python program (no native code, no FFI).  Each entry
+ * point below replaces one piece of its simulation call stack, cited by file
+ * and line in the reference project:
+ *
+ *   mcl_k_*  the event-driven kinetics loop of simulate()
+ *            src/class/simulate.py:36-92 over TLTrapSim / Box / Physics
+ *            (src/class/tl_trap_lab.py:27-60, src/class/engine.py:44-188).
+ *   mcl_b_*  the fixed-dt Bernoulli kinetics over ragged batches of parameter
+ *            sets (the dilute limit of the same physics; no single reference
+ *            function -- it replaces the per-set loop that
+ *            src/class/optimizer.py:68-84 and simulate.py:36-48 run serially).
+ *   mcl_graph_*  CUDA-graph capture/replay of a packed batch (no reference
+ *            counterpart; the reference re-enters Python per step).
+ */
+#ifndef MCLUM_H
+#define MCLUM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCL_ABI_VERSION 1
+
+/* ---- return / status codes ------------------------------------------- */
+#define MCL_OK 0
+#define MCL_EINVAL (-1)     /* bad argument (host-side validation)          */
+#define MCL_ECAPACITY (-2)  /* an output table or on-chip buffer too small   */
+#define MCL_EBUDGET (-3)    /* a step / iteration budget ran out             */
+#define MCL_ECUDA (-4)      /* a CUDA runtime call failed                    */
+#define MCL_ENODEV (-5)     /* no usable sm_103 device                        */
+#define MCL_ENOHOLE (-6)    /* a nearest-centre search over zero centres      */
+
+/* ---- precision / RNG selectors ---------------------------------------- */
+#define MCL_FP32 0          /* FP32 arithmetic, 32-bit Philox uniforms        */
+#define MCL_FP64 1          /* FP64 arithmetic, 53-bit Philox uniforms        */
+#define MCL_RNG_PHILOX 0    /* counter-based Philox4x32-10 keyed by seed      */
+#define MCL_RNG_INJECTED 1  /* caller-supplied uniforms (FP64 only)           */
+
+/* ---- Bernoulli-mode schedule ------------------------------------------ */
+#define MCL_SEG_THERMAL 1   /* add s*exp(-E/(k_b*T)) to the segment's rate   */
+
+/* One phase of a set's schedule (TL ramp, isothermal hold, irradiation,
+ * fading, optical stimulation).  Step j of the segment has length
+ * dt*g^j (g = dt_growth), starts at time t_j = sum of earlier lengths, at
+ * temperature T0 + beta*t_j, with escape rate
+ *     A_j = rate_const + [flags&THERMAL] s*exp(-E/(k_b*T))
+ * scaled per trap by exp(-alpha*r'), and fill probability
+ * 1-exp(-dt_j*fill_rate) for empty traps.  Events of step j count into bin
+ * bin_offset + j/steps_per_bin of the set.                          64 B */
+typedef struct mcl_segment {
+  int32_t n_steps;
+  int32_t steps_per_bin;
+  int32_t bin_offset;
+  int32_t flags;
+  double dt;
+  double dt_growth;
+  double T0;
+  double beta;
+  double rate_const;
+  double fill_rate;
+} mcl_segment;
+
+/* One parameter set: n_slots traps, the first n_filled of them occupied at
+ * the start, segments [seg_begin, seg_begin+seg_count).                88 B */
+typedef struct mcl_set {
+  int32_t n_slots;
+  int32_t n_filled;
+  int32_t seg_begin;
+  int32_t seg_count;
+  int32_t n_bins;
+  uint32_t set_id;      /* Philox counter word 2 (the set's identity)        */
+  int64_t bin_offset;   /* first bin of this set in lum[] / alive[]          */
+  int64_t slot_offset;  /* first slot of this set in fates[]                  */
+  int64_t u_offset;     /* injected mode: first uniform of this set           */
+  int64_t total_steps;  /* sum of the segments' n_steps                       */
+  double E;             /* trap depth, eV                                     */
+  double s;             /* frequency factor, 1/s                              */
+  double alpha;         /* tunnelling coefficient on the dimensionless r'     */
+  double k_b;           /* Boltzmann constant, eV/K                            */
+} mcl_set;
+
+/* A work item: slots [slot_begin, slot_begin + slots_per_item) of one set. */
+typedef struct mcl_item {
+  int32_t set;
+  int32_t slot_begin;
+} mcl_item;
+
+/* Arguments of one Bernoulli launch (all pointers are device pointers). */
+typedef struct mcl_b_args {
+  const mcl_set* sets;
+  const mcl_segment* segs;
+  const mcl_item* items;
+  uint32_t* lum;           /* [n_bins_total] recombinations per bin           */
+  uint32_t* alive;         /* [n_bins_total] filled traps at bin end, or NULL */
+  int32_t* fates;          /* [n_slots_total] step of last recombination, or NULL */
+  const double* uniforms;  /* injected mode only                              */
+  int32_t* status;         /* [1] device status word                          */
+  void* workspace;         /* mcl_b_workspace_size() bytes of device scratch  */
+  int64_t n_bins_total;
+  int64_t n_slots_total;
+  uint64_t seed;
+  int32_t n_sets;
+  int32_t n_segs;
+  int32_t n_items;
+  int32_t slots_per_item;  /* block * ept                                      */
+  int32_t max_bins;        /* largest n_bins of any set                        */
+  int32_t precision;       /* MCL_FP32 | MCL_FP64                               */
+  int32_t rng;             /* MCL_RNG_PHILOX | MCL_RNG_INJECTED                 */
+  int32_t block;           /* threads per CTA: 128, 256 or 512                  */
+  int32_t ept;             /* slots per thread: 1, 2, 4 or 8                    */
+  int32_t grid;            /* persistent CTAs; 0 = SM count x occupancy         */
+  int32_t zero_outputs;    /* 1: clear lum/alive/fates/status before the launch */
+  int32_t reserved;
+} mcl_b_args;
+
+/* ---- library ------------------------------------------------------------ */
+int mcl_abi_version(void);
+const char* mcl_status_string(int code);
+/* Text of the last CUDA error seen by this thread's calls ("" if none). */
+const char* mcl_last_error(void);
+/* sizeof(mcl_segment), sizeof(mcl_set), sizeof(mcl_item), sizeof(mcl_b_args),
+ * written to out[0..3], so bindings can check their struct layouts. */
+int mcl_struct_sizes(size_t* out);
+/* SM count and compute capability of the current device. */
+int mcl_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* ---- Bernoulli mode ----------------------------------------------------- */
+/* Host-side validation of a packed batch (host arrays). */
+int mcl_b_validate(const mcl_set* sets, int32_t n_sets, const mcl_segment* segs,
+                   int32_t n_segs, int64_t n_bins_total, int64_t n_slots_total,
+                   int32_t precision, int32_t rng, int64_t n_uniforms);
+/* Ragged packer: split every set into items of slots_per_item slots, ordered
+ * longest-first (steps x slots) for the persistent ticket scheduler.  Writes
+ * at most items_cap items and returns the item count (or a negative code). */
+int64_t mcl_b_pack_items(const mcl_set* sets, int32_t n_sets, int32_t slots_per_item,
+                         mcl_item* items_out, int64_t items_cap);
+/* Bytes of device workspace one launch needs. */
+size_t mcl_b_workspace_size(void);
+/* Largest block/ept-independent dynamic shared memory (bytes) for max_bins. */
+size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t want_alive);
+/* Launch on `stream` (stream-ordered, no host synchronisation). */
+int mcl_b_run(const mcl_b_args* args, void* stream);
+
+/* ---- CUDA graphs -------------------------------------------------------- */
+/* Capture mcl_b_run(args) (with its output clearing) into a graph. */
+int mcl_b_graph_create(const mcl_b_args* args, void* stream, void** graph_out);
+int mcl_graph_launch(void* graph, void* stream);
+int mcl_graph_destroy(void* graph);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCLUM_H */

@@ -1,0 +1,141 @@
+"""ctypes binding of ``libmclum.so`` (the C ABI declared in include/mclum.h).
+
+The library is built in-tree by ``mcluminescence_gb300.build``.  There is no
+CPU fallback: if the library is missing or fails to load, every entry point
+raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+MCL_OK = 0
+MCL_EINVAL = -1
+MCL_ECAPACITY = -2
+MCL_EBUDGET = -3
+MCL_ECUDA = -4
+MCL_ENODEV = -5
+MCL_ENOHOLE = -6
+
+MCL_FP32 = 0
+MCL_FP64 = 1
+MCL_RNG_PHILOX = 0
+MCL_RNG_INJECTED = 1
+MCL_SEG_THERMAL = 1
+
+# numpy mirrors of the C structs (natural alignment, little endian)
+SEG_DTYPE = np.dtype([
+    ("n_steps", "<i4"), ("steps_per_bin", "<i4"), ("bin_offset", "<i4"), ("flags", "<i4"),
+    ("dt", "<f8"), ("dt_growth", "<f8"), ("T0", "<f8"), ("beta", "<f8"),
+    ("rate_const", "<f8"), ("fill_rate", "<f8")], align=True)
+SET_DTYPE = np.dtype([
+    ("n_slots", "<i4"), ("n_filled", "<i4"), ("seg_begin", "<i4"), ("seg_count", "<i4"),
+    ("n_bins", "<i4"), ("set_id", "<u4"), ("bin_offset", "<i8"), ("slot_offset", "<i8"),
+    ("u_offset", "<i8"), ("total_steps", "<i8"), ("E", "<f8"), ("s", "<f8"),
+    ("alpha", "<f8"), ("k_b", "<f8")], align=True)
+ITEM_DTYPE = np.dtype([("set", "<i4"), ("slot_begin", "<i4")], align=True)
+
+
+class BArgs(C.Structure):
+    _fields_ = [
+        ("sets", C.c_void_p), ("segs", C.c_void_p), ("items", C.c_void_p),
+        ("lum", C.c_void_p), ("alive", C.c_void_p), ("fates", C.c_void_p),
+        ("uniforms", C.c_void_p), ("status", C.c_void_p), ("workspace", C.c_void_p),
+        ("n_bins_total", C.c_int64), ("n_slots_total", C.c_int64), ("seed", C.c_uint64),
+        ("n_sets", C.c_int32), ("n_segs", C.c_int32), ("n_items", C.c_int32),
+        ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
+        ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
+        ("zero_outputs", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class MclError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        lib = _LIB[0]
+        msg = lib.mcl_status_string(code).decode() if lib is not None else str(code)
+        extra = lib.mcl_last_error().decode() if (lib is not None and code == MCL_ECUDA) else ""
+        super().__init__(f"{what}: {msg}" + (f" ({extra})" if extra else ""))
+
+
+_LIB = [None]
+_LOCK = threading.Lock()
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def _declare(lib):
+    vp, i32, i64, u64, sz = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_size_t
+    sig = {
+        "mcl_abi_version": (C.c_int, []),
+        "mcl_status_string": (C.c_char_p, [C.c_int]),
+        "mcl_last_error": (C.c_char_p, []),
+        "mcl_struct_sizes": (C.c_int, [C.POINTER(sz)]),
+        "mcl_device_info": (C.c_int, [C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+        "mcl_b_validate": (C.c_int, [vp, i32, vp, i32, i64, i64, i32, i32, i64]),
+        "mcl_b_pack_items": (i64, [vp, i32, i32, vp, i64]),
+        "mcl_b_workspace_size": (sz, []),
+        "mcl_b_smem_bytes": (sz, [i32, i32, i32]),
+        "mcl_b_run": (C.c_int, [C.POINTER(BArgs), vp]),
+        "mcl_b_graph_create": (C.c_int, [C.POINTER(BArgs), vp, C.POINTER(vp)]),
+        "mcl_graph_launch": (C.c_int, [vp, vp]),
+        "mcl_graph_destroy": (C.c_int, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+EXPORTS = (
+    "mcl_abi_version", "mcl_status_string", "mcl_last_error", "mcl_struct_sizes",
+    "mcl_device_info", "mcl_b_validate", "mcl_b_pack_items", "mcl_b_workspace_size",
+    "mcl_b_smem_bytes", "mcl_b_run", "mcl_b_graph_create", "mcl_graph_launch",
+    "mcl_graph_destroy",
+)
+
+
+def load(auto_build: bool = False):
+    """Load (optionally building first) the CUDA library; raises if absent."""
+    with _LOCK:
+        if _LIB[0] is not None:
+            return _LIB[0]
+        path = lib_path()
+        if auto_build:
+            _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"CUDA library {path} is not built; run `python -c \"import __graft_entry__ as g; "
+                f"g.build()\"` or `python -m mcluminescence_gb300.build` (there is no CPU fallback)")
+        lib = _declare(C.CDLL(path))
+        if lib.mcl_abi_version() != 1:
+            raise RuntimeError("libmclum ABI version mismatch; rebuild the library")
+        sizes = (C.c_size_t * 4)()
+        lib.mcl_struct_sizes(sizes)
+        want = (SEG_DTYPE.itemsize, SET_DTYPE.itemsize, ITEM_DTYPE.itemsize, C.sizeof(BArgs))
+        if tuple(sizes) != want:
+            raise RuntimeError(f"struct layout mismatch: library {tuple(sizes)} vs binding {want}")
+        _LIB[0] = lib
+        return lib
+
+
+def check(code: int, what: str) -> None:
+    if code != MCL_OK:
+        raise MclError(code, what)
+
+
+def ptr(arr) -> int:
+    """Device (torch tensor) or host (numpy array) data pointer, or 0 for None."""
+    if arr is None:
+        return 0
+    if isinstance(arr, np.ndarray):
+        return arr.ctypes.data
+    return arr.data_ptr()

@@ -1,0 +1,77 @@
+"""Launch-shape autotuner for the Bernoulli kernel.
+
+Times each (threads per CTA, traps per thread) candidate with CUDA events on a
+deterministic sample of the batch (every 32nd set, so the ragged size and step
+mix is kept) and caches the winner per (device, precision, shape bucket) in a
+JSON file next to the library.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+from typing import Sequence, Tuple
+
+from . import build as _build
+from .schedule import SetSpec
+
+CANDIDATES = {
+    "fp32": [(256, 4), (256, 2), (128, 4), (512, 2), (256, 8), (128, 8), (512, 4), (256, 1)],
+    "fp64": [(256, 1), (256, 2)],
+}
+CACHE = os.path.join(_build.LIBDIR, "autotune.json")
+
+
+def _bucket(specs: Sequence[SetSpec], precision: str) -> str:
+    import torch
+    mb = max(s.n_bins for s in specs)
+    steps = sum(s.total_steps for s in specs) / max(len(specs), 1)
+    slots = sum(s.n_slots for s in specs) / max(len(specs), 1)
+    return (f"{torch.cuda.get_device_name()}|{precision}|bins{2 ** math.ceil(math.log2(max(mb, 1)))}"
+            f"|steps{2 ** round(math.log2(max(steps, 1)))}|slots{2 ** round(math.log2(max(slots, 1)))}")
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def time_shape(specs, precision, block, ept, reps=2) -> float:
+    import torch
+    from .batch import BernoulliBatch
+    b = BernoulliBatch(specs, precision=precision, seed=1, block=block, ept=ept, want_alive=True)
+    s = torch.cuda.Stream()
+    b.capture(s)
+    b.replay(s)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        b.replay(s)
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
+                   use_cache: bool = True) -> Tuple[int, int]:
+    key = _bucket(specs, precision)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        return tuple(cache[key]["best"])
+    sample = list(specs[::32]) or list(specs)
+    times = {}
+    for blk, ept in CANDIDATES[precision]:
+        times[(blk, ept)] = time_shape(sample, precision, blk, ept)
+    best = min(times, key=times.get)
+    cache = _load()
+    cache[key] = {"best": list(best), "ms": {f"{b}x{e}": t for (b, e), t in times.items()}}
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        with open(CACHE, "w") as f:
+            json.dump(cache, f, indent=1)
+    except OSError:
+        pass
+    return best
