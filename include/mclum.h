@@ -74,7 +74,9 @@ typedef struct mcl_segment {
 } mcl_segment;
 
 /* One parameter set: n_slots traps, the first n_filled of them occupied at
- * the start, segments [seg_begin, seg_begin+seg_count).                88 B */
+ * the start, segments [seg_begin, seg_begin+seg_count).  step_offset is the
+ * set's first entry in the per-step rate table kept in the workspace; sets
+ * must be laid out back to back (step_offset = sum of earlier total_steps). 96 B */
 typedef struct mcl_set {
   int32_t n_slots;
   int32_t n_filled;
@@ -86,6 +88,7 @@ typedef struct mcl_set {
   int64_t slot_offset;  /* first slot of this set in fates[]                  */
   int64_t u_offset;     /* injected mode: first uniform of this set           */
   int64_t total_steps;  /* sum of the segments' n_steps                       */
+  int64_t step_offset;  /* first step of this set in the rate table           */
   double E;             /* trap depth, eV                                     */
   double s;             /* frequency factor, 1/s                              */
   double alpha;         /* tunnelling coefficient on the dimensionless r'     */
@@ -108,7 +111,9 @@ typedef struct mcl_b_args {
   int32_t* fates;          /* [n_slots_total] step of last recombination, or NULL */
   const double* uniforms;  /* injected mode only                              */
   int32_t* status;         /* [1] device status word                          */
-  void* workspace;         /* mcl_b_workspace_size() bytes of device scratch  */
+  void* workspace;         /* device scratch: ticket + per-step rate table      */
+  int64_t workspace_bytes; /* >= mcl_b_workspace_size(sets, n_sets, precision) */
+  int64_t table_steps;     /* sum of total_steps over all sets (table rows)    */
   int64_t n_bins_total;
   int64_t n_slots_total;
   uint64_t seed;
@@ -147,8 +152,10 @@ int mcl_b_validate(const mcl_set* sets, int32_t n_sets, const mcl_segment* segs,
  * at most items_cap items and returns the item count (or a negative code). */
 int64_t mcl_b_pack_items(const mcl_set* sets, int32_t n_sets, int32_t slots_per_item,
                          mcl_item* items_out, int64_t items_cap);
-/* Bytes of device workspace one launch needs. */
-size_t mcl_b_workspace_size(void);
+/* Bytes of device workspace one launch needs (host set array): a 256-byte
+ * header (the work ticket) plus one table entry per step of every set
+ * (c_j and q_j: 8 bytes in FP32 mode, 16 in FP64 mode). */
+size_t mcl_b_workspace_size(const mcl_set* sets, int32_t n_sets, int32_t precision);
 /* Largest block/ept-independent dynamic shared memory (bytes) for max_bins. */
 size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t want_alive);
 /* Launch on `stream` (stream-ordered, no host synchronisation). */

@@ -36,7 +36,7 @@ SEG_DTYPE = np.dtype([
 SET_DTYPE = np.dtype([
     ("n_slots", "<i4"), ("n_filled", "<i4"), ("seg_begin", "<i4"), ("seg_count", "<i4"),
     ("n_bins", "<i4"), ("set_id", "<u4"), ("bin_offset", "<i8"), ("slot_offset", "<i8"),
-    ("u_offset", "<i8"), ("total_steps", "<i8"), ("E", "<f8"), ("s", "<f8"),
+    ("u_offset", "<i8"), ("total_steps", "<i8"), ("step_offset", "<i8"), ("E", "<f8"), ("s", "<f8"),
     ("alpha", "<f8"), ("k_b", "<f8")], align=True)
 ITEM_DTYPE = np.dtype([("set", "<i4"), ("slot_begin", "<i4")], align=True)
 
@@ -46,7 +46,7 @@ class BArgs(C.Structure):
         ("sets", C.c_void_p), ("segs", C.c_void_p), ("items", C.c_void_p),
         ("lum", C.c_void_p), ("alive", C.c_void_p), ("fates", C.c_void_p),
         ("uniforms", C.c_void_p), ("status", C.c_void_p), ("workspace", C.c_void_p),
-        ("n_bins_total", C.c_int64), ("n_slots_total", C.c_int64), ("seed", C.c_uint64),
+        ("workspace_bytes", C.c_int64), ("table_steps", C.c_int64), ("n_bins_total", C.c_int64), ("n_slots_total", C.c_int64), ("seed", C.c_uint64),
         ("n_sets", C.c_int32), ("n_segs", C.c_int32), ("n_items", C.c_int32),
         ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
         ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
@@ -81,7 +81,7 @@ def _declare(lib):
         "mcl_device_info": (C.c_int, [C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
         "mcl_b_validate": (C.c_int, [vp, i32, vp, i32, i64, i64, i32, i32, i64]),
         "mcl_b_pack_items": (i64, [vp, i32, i32, vp, i64]),
-        "mcl_b_workspace_size": (sz, []),
+        "mcl_b_workspace_size": (sz, [vp, i32, i32]),
         "mcl_b_smem_bytes": (sz, [i32, i32, i32]),
         "mcl_b_run": (C.c_int, [C.POINTER(BArgs), vp]),
         "mcl_b_graph_create": (C.c_int, [C.POINTER(BArgs), vp, C.POINTER(vp)]),

@@ -16,7 +16,7 @@ from . import build as _build
 from .schedule import SetSpec
 
 CANDIDATES = {
-    "fp32": [(256, 4), (256, 2), (128, 4), (512, 2), (256, 8), (128, 8), (512, 4), (256, 1)],
+    "fp32": [(256, 4), (256, 2), (128, 4), (128, 2), (256, 8), (128, 8)],
     "fp64": [(256, 1), (256, 2)],
 }
 CACHE = os.path.join(_build.LIBDIR, "autotune.json")

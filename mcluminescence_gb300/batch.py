@@ -45,6 +45,7 @@ def pack_host(specs: Sequence[SetSpec]):
     s_off = np.zeros(n_sets + 1, dtype=np.int64)
     u_off = np.zeros(n_sets + 1, dtype=np.int64)
     g = 0
+    t_off = 0
     for i, sp in enumerate(specs):
         sp.finalize()
         rec = sets[i]
@@ -58,6 +59,8 @@ def pack_host(specs: Sequence[SetSpec]):
         rec["slot_offset"] = s_off[i]
         rec["u_offset"] = u_off[i]
         rec["total_steps"] = sp.total_steps
+        rec["step_offset"] = t_off
+        t_off += sp.total_steps
         rec["E"], rec["s"], rec["alpha"], rec["k_b"] = sp.E, sp.s, sp.alpha, sp.k_b
         for sg in sp.segments:
             r = segs[g]
@@ -141,7 +144,9 @@ class BernoulliBatch:
         self.d_u = (torch.from_numpy(np.ascontiguousarray(uniforms[:n_u], dtype=np.float64)).to(dev)
                     if self.rng == _lib.MCL_RNG_INJECTED else None)
         self.d_status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.d_ws = torch.zeros(int(self.lib.mcl_b_workspace_size()), dtype=torch.uint8, device=dev)
+        self.table_steps = int(sum(sp.total_steps for sp in self.specs))
+        self.ws_bytes = int(self.lib.mcl_b_workspace_size(_lib.ptr(sets), len(sets), self.precision))
+        self.d_ws = torch.zeros(self.ws_bytes, dtype=torch.uint8, device=dev)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
         self._graph = None
         self.args = self._make_args(zero_outputs=1)
@@ -153,6 +158,7 @@ class BernoulliBatch:
         a.lum, a.alive, a.fates = _lib.ptr(self.d_lum), _lib.ptr(self.d_alive), _lib.ptr(self.d_fates)
         a.uniforms = _lib.ptr(self.d_u)
         a.status, a.workspace = _lib.ptr(self.d_status), _lib.ptr(self.d_ws)
+        a.workspace_bytes, a.table_steps = self.ws_bytes, self.table_steps
         a.n_bins_total, a.n_slots_total, a.seed = self.n_bins_total, self.n_slots_total, self.seed
         a.n_sets, a.n_segs, a.n_items = len(self.host_sets), len(self.host_segs), self.n_items
         a.slots_per_item, a.max_bins = self.block * self.ept, self.max_bins

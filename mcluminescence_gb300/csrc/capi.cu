@@ -72,8 +72,11 @@ extern "C" int mcl_b_validate(const mcl_set* sets, int32_t n_sets, const mcl_seg
   if (precision != MCL_FP32 && precision != MCL_FP64) return MCL_EINVAL;
   if (rng != MCL_RNG_PHILOX && rng != MCL_RNG_INJECTED) return MCL_EINVAL;
   if (rng == MCL_RNG_INJECTED && precision != MCL_FP64) return MCL_EINVAL;
+  int64_t step_prefix = 0;
   for (int32_t i = 0; i < n_sets; ++i) {
     const mcl_set& s = sets[i];
+    if (s.step_offset != step_prefix) return MCL_EINVAL;
+    step_prefix += s.total_steps;
     if (s.n_slots < 0 || s.n_filled < 0 || s.n_filled > s.n_slots) return MCL_EINVAL;
     if (s.seg_count < 0 || s.seg_begin < 0 || (int64_t)s.seg_begin + s.seg_count > n_segs) return MCL_EINVAL;
     if (s.n_bins < 0 || s.bin_offset < 0 || s.bin_offset + s.n_bins > n_bins_total) return MCL_ECAPACITY;

@@ -19,6 +19,7 @@ constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
 constexpr uint32_t kTagStep = 0;    // per-step Bernoulli uniforms
 constexpr uint32_t kTagInit = 1;    // initial nearest-centre distance r'
 constexpr uint32_t kTagRefill = 2;  // r' of a trap refilled at a step
+constexpr uint32_t kTagLow = 3;     // low 16 bits of an FP32-mode uniform
 
 __device__ __forceinline__ uint4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2,
                                                uint32_t c3, uint32_t k0, uint32_t k1) {

@@ -9,25 +9,32 @@
 // recombination photon, counted into the set's bin for that step.
 //
 // Execution:
-// * a persistent grid pulls work items (set, 'slots_per_item' consecutive
-//   trap slots) from an atomic ticket; items are packed longest-first on the
-//   host, so the ticket order is a longest-processing-time schedule;
-// * each thread owns `EPT` slots: their w and filled bits live in registers,
-//   and the electrons themselves are never stored in memory -- r' comes from
-//   the Philox stream keyed by (set, slot), every step's uniform from
-//   (set, slot, step);
-// * per step, c_j (the same for every slot of the set) is read from a
-//   shared-memory chunk the CTA precomputes in FP64;
-// * FP32 mode tests every electron-step with three ALU ops: the top 23 bits
-//   of the uniform form f in [1,2); if f >= 1 + c*w + 2^-21 the uniform is
-//   provably >= c*w >= p and nothing happens.  Otherwise (probability
-//   ~ c*w + 2^-21) the exact test u32 < ceil(p * 2^32) with p = -expm1f(-c*w)
-//   decides;
-// * events accumulate in a per-thread counter, are summed per warp with a
-//   single reduction at every bin boundary, added to shared-memory bins, and
-//   the CTA adds each non-zero bin to HBM with one atomic when the item ends.
-// HBM traffic is therefore the set/segment/item descriptors in and the bins
-// out; the kernel is bound by integer/FP32 issue (the Philox rounds).
+// * a pre-pass (kb_tables) evaluates c_j and q_j once per step of every set,
+//   in FP64, into a table in the workspace (the only FP64 work of a launch);
+// * a persistent grid pulls work items (set, `block*ept` consecutive trap
+//   slots) from an atomic ticket; items are packed longest-first on the host,
+//   so the ticket order is a longest-processing-time schedule;
+// * each thread owns `EPT` slots: their w and filled bits live in registers.
+//   Electrons are never stored: r' comes from the Philox stream keyed by
+//   (set, slot), every step's uniform from (set, slot, step).  The Philox key
+//   schedule is precomputed on the host and read from the kernel's constant
+//   parameter bank, so the rounds cost only the multiplies and 3-input XORs;
+// * the CTA copies 256-step chunks of (c_j, q_j) into shared memory;
+// * FP32 mode spends 16 random bits per electron-step in the common case: a
+//   Philox block (four 32-bit words) covers 8 steps of a slot.  The step's
+//   16-bit field h becomes f = 1 + h 2^-16 with one logic op (a byte permute
+//   first for the upper four steps); d = (f - K) - c w (an FADD and an FFMA,
+//   K = 1 + 2^-21).  d >= 0 proves u >= c w >= p, so nothing happens.  The
+//   sign bits of all slots of a step are OR-ed and one branch per step enters
+//   the exact test, which draws the uniform's low 16 bits from a separate
+//   Philox counter and checks u32 < ceil(p 2^32), p = -expm1f(-c w); it runs
+//   with probability ~ c w + 2^-16.  Halving the Philox work per trial this
+//   way matters because the 32x32->64 multiplies of the Philox rounds occupy
+//   the FMA-heavy pipe, the kernel's binding unit;
+// * events are added to shared-memory bins (rare); at each bin end the warp
+//   sums the filled-trap counts with one reduction; when an item ends the CTA
+//   adds every non-zero bin to HBM with one atomic.
+// HBM traffic: descriptors, the step table (L2-resident per set) and bins.
 
 #include <algorithm>
 #include <cstdio>
@@ -37,15 +44,40 @@
 namespace mcl {
 namespace {
 
-constexpr int kChunk = 256;  // steps whose c_j/q_j one shared-memory chunk holds
+constexpr int kChunk = 256;       // steps per shared-memory chunk of (c_j, q_j)
+constexpr int kHeaderBytes = 256;  // workspace header (ticket)
 
-struct Workspace {
+struct Header {
   int32_t ticket;
-  int32_t pad[63];
 };
 
-// c_j and q_j of local step j of segment sg (FP64, no contraction so that the
-// values match the oracle's numpy evaluation order).
+// Kernel parameters: the public launch arguments plus the Philox key
+// schedule k + r*W (r = 0..9), which lands in the constant parameter bank.
+struct KParams {
+  mcl_b_args a;
+  uint32_t ks0[10];
+  uint32_t ks1[10];
+};
+
+// Philox4x32-10 with a precomputed key schedule.
+__device__ __forceinline__ uint4 philox_ks(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                           const KParams& p) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)kPhiloxM0 * c0;
+    const uint64_t p1 = (uint64_t)kPhiloxM1 * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ p.ks0[r];
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ p.ks1[r];
+    c1 = (uint32_t)p1;
+    c3 = (uint32_t)p0;
+    c0 = n0;
+    c2 = n2;
+  }
+  return make_uint4(c0, c1, c2, c3);
+}
+
+// c_j and q_j of local step j of segment sg (FP64 without contraction, in the
+// oracle's evaluation order).
 __device__ __forceinline__ void step_constants(const mcl_set& st, const mcl_segment& sg, int j,
                                                double& c, double& q) {
   double dtj, t;
@@ -66,8 +98,52 @@ __device__ __forceinline__ void step_constants(const mcl_set& st, const mcl_segm
   q = sg.fill_rate > 0.0 ? -expm1(__dmul_rn(-dtj, sg.fill_rate)) : 0.0;
 }
 
+// Pre-pass: one CTA per set fills its rows of the (c_j, q_j) table.
+template <typename T>
+__global__ void __launch_bounds__(256) kb_tables(const mcl_b_args a) {
+  const int s = blockIdx.x;
+  if (s >= a.n_sets) return;
+  const mcl_set st = a.sets[s];
+  T* tab = reinterpret_cast<T*>(reinterpret_cast<char*>(a.workspace) + kHeaderBytes) + 2 * st.step_offset;
+  int64_t base = 0;
+  for (int g = 0; g < st.seg_count; ++g) {
+    const mcl_segment sg = a.segs[st.seg_begin + g];
+    for (int j = threadIdx.x; j < sg.n_steps; j += blockDim.x) {
+      double c, q;
+      step_constants(st, sg, j, c, q);
+      tab[2 * (base + j)] = (T)c;
+      tab[2 * (base + j) + 1] = (T)q;
+    }
+    base += sg.n_steps;
+  }
+}
+
 __device__ __forceinline__ float r_prime_f(float u) { return cbrtf(-log1pf(-u)); }
 __device__ __forceinline__ double r_prime_d(double u) { return cbrt(-log1p(-u)); }
+
+// Exact FP32-mode tests, kept out of line: they run on ~2e-5 of the trials.
+// The 32-bit uniform of a trial is (h << 16) | lo16: h is the 16-bit field the
+// fast test used, lo16 the low half of word 0 of philox(step, slot, set,
+// TAG_LO), drawn only here.
+__device__ __noinline__ uint32_t full_u32(uint32_t h, uint32_t kstep, uint32_t slot, uint32_t set_id,
+                                          const KParams& P) {
+  const uint4 r = philox_ks(kstep, slot, set_id, kTagLow, P);
+  return (h << 16) | (r.x & 0xffffu);
+}
+
+__device__ __noinline__ bool escape_exact(uint32_t u32, float c, float w) {
+  const float p = -expm1f(-__fmul_rn(c, w));
+  return p >= 1.0f || u32 < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
+}
+
+__device__ __noinline__ bool threshold_exact(uint32_t u32, float q) {
+  return q >= 1.0f || u32 < __float2uint_ru(__fmul_rn(q, 4294967296.0f));
+}
+
+__device__ __noinline__ float refill_w(uint32_t word, float alpha) {
+  const float u = (float)(word >> 8) * 0x1p-24f;
+  return expf(-alpha * r_prime_f(u));
+}
 
 // Sum `v` over the warp and add it to *dst from lane 0 (skipped if all zero).
 __device__ __forceinline__ void warp_flush(uint32_t v, uint32_t* dst) {
@@ -102,26 +178,149 @@ __device__ __forceinline__ uint32_t word_of(const uint4& r, int q) {
   return q == 0 ? r.x : (q == 1 ? r.y : (q == 2 ? r.z : r.w));
 }
 
+// Step t (0..7) of a Philox block uses a 16-bit field h of word t&3: bits
+// 22..7 of the word for t < 4, bits 22..7 of the word rotated by 16 for t >= 4.
+// fast_f returns 1 + h * 2^-16 by dropping the field into a float's mantissa.
+template <int T>
+__device__ __forceinline__ float fast_f(uint32_t word) {
+  const uint32_t x = (T < 4) ? word : __byte_perm(word, 0, 0x1032);
+  return __uint_as_float((x & 0x007fff80u) | 0x3f800000u);
+}
+
+template <int T>
+__device__ __forceinline__ uint32_t field16(uint32_t word) {
+  const uint32_t x = (T < 4) ? word : __byte_perm(word, 0, 0x1032);
+  return (x >> 7) & 0xffffu;
+}
+
+// Per-thread state of the FP32 kernel for one work item.
+template <int EPT>
+struct SlotState {
+  float w[EPT];        // w of a filled trap, 0 for an empty one
+  uint32_t slot[EPT];  // slot index within the set
+  uint32_t filled;     // bit i: slot i holds an electron
+};
+
+// One step (index T within its Philox block) for all EPT slots.
+template <int EPT, bool FILL, int T>
+__device__ __forceinline__ void step_f32(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                         const uint4 (&r)[EPT], float c, float qf, int64_t kstep,
+                                         uint32_t* s_lum, int bin, float alpha) {
+  constexpr float kMargin = 1.0f + 0x1p-21f;
+  float d[EPT];
+  uint32_t any = 0;
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    const float fk = fast_f<T>(word_of(r[i], T & 3)) - kMargin;
+    if (FILL && !((S.filled >> i) & 1u)) {
+      d[i] = fk - qf;
+    } else {
+      d[i] = __fmaf_rn(-c, S.w[i], fk);
+    }
+    any |= __float_as_uint(d[i]);
+  }
+  if ((int32_t)any < 0) {
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      if ((int32_t)__float_as_uint(d[i]) < 0) {
+        const uint32_t h = field16<T>(word_of(r[i], T & 3));
+        if ((S.filled >> i) & 1u) {
+          const uint32_t u32 = full_u32(h, (uint32_t)kstep, S.slot[i], st.set_id, P);
+          if (escape_exact(u32, c, S.w[i])) {
+            S.filled &= ~(1u << i);
+            S.w[i] = 0.0f;
+            atomicAdd(&s_lum[bin], 1u);
+            if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)kstep;
+          }
+        } else if (FILL && S.slot[i] < (uint32_t)st.n_slots) {
+          const uint32_t u32 = full_u32(h, (uint32_t)kstep, S.slot[i], st.set_id, P);
+          if (threshold_exact(u32, qf)) {
+            const uint4 rr = philox_ks((uint32_t)kstep, S.slot[i], st.set_id, kTagRefill, P);
+            S.w[i] = refill_w(rr.x, alpha);
+            S.filled |= 1u << i;
+          }
+        }
+      }
+    }
+  }
+}
+
+// The steps of one Philox block (8 steps; fewer at a segment's end when
+// FULL is false) starting at chunk index jq.
+template <int EPT, bool FILL, bool FULL>
+__device__ __forceinline__ void block_f32(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                          uint32_t blk, const float* s_c, const float* s_q, int jq,
+                                          int nq, int64_t kstep, uint32_t* s_lum, uint32_t* s_alive,
+                                          int& bin, int& to_flush, int spb, int remaining_after,
+                                          float alpha) {
+  uint4 r[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
+#define MCL_STEP(T)                                                                              \
+  if (FULL || (T) < nq) {                                                                        \
+    step_f32<EPT, FILL, T>(P, st, S, r, s_c[jq + (T)], FILL ? s_q[jq + (T)] : 0.0f, kstep + (T), \
+                           s_lum, bin, alpha);                                                   \
+    if (--to_flush == 0) {                                                                       \
+      if (s_alive) warp_flush((uint32_t)__popc(S.filled), &s_alive[bin]);                        \
+      ++bin;                                                                                     \
+      to_flush = min(spb, remaining_after - (T));                                                \
+    }                                                                                            \
+  }
+  MCL_STEP(0) MCL_STEP(1) MCL_STEP(2) MCL_STEP(3) MCL_STEP(4) MCL_STEP(5) MCL_STEP(6) MCL_STEP(7)
+#undef MCL_STEP
+}
+
+// One segment of one work item (FP32).
+template <int BLOCK, int EPT, bool FILL>
+__device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st, const mcl_segment& sg,
+                                            SlotState<EPT>& S, const float2* tab, float* s_c, float* s_q,
+                                            uint32_t* s_lum, uint32_t* s_alive, uint32_t bbase,
+                                            int64_t kglob, float alpha) {
+  const int spb = sg.steps_per_bin;
+  int bin = sg.bin_offset;
+  int to_flush = min(spb, sg.n_steps);
+  for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
+    const int nj = min(kChunk, sg.n_steps - j0);
+    __syncthreads();
+    for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
+      const float2 cq = tab[j0 + jj];
+      s_c[jj] = cq.x;
+      s_q[jj] = cq.y;
+    }
+    __syncthreads();
+    int jq = 0;
+    for (; jq + 8 <= nj; jq += 8) {
+      block_f32<EPT, FILL, true>(P, st, S, bbase + (uint32_t)((j0 + jq) >> 3), s_c, s_q, jq, 8,
+                                 kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
+                                 sg.n_steps - (j0 + jq) - 1, alpha);
+    }
+    if (jq < nj) {  // the segment's last, partial Philox block
+      block_f32<EPT, FILL, false>(P, st, S, bbase + (uint32_t)((j0 + jq) >> 3), s_c, s_q, jq, nj - jq,
+                                  kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
+                                  sg.n_steps - (j0 + jq) - 1, alpha);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FP32 / Philox kernel
 // ---------------------------------------------------------------------------
 template <int BLOCK, int EPT>
-__global__ void __launch_bounds__(BLOCK) kb_f32(const mcl_b_args a) {
+__global__ void __launch_bounds__(BLOCK) kb_f32(const KParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const mcl_b_args& a = P.a;
   float* s_c = reinterpret_cast<float*>(smem);
   float* s_q = s_c + kChunk;
   uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
   uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
   __shared__ int s_item;
 
-  Workspace* ws = reinterpret_cast<Workspace*>(a.workspace);
+  Header* hdr = reinterpret_cast<Header*>(a.workspace);
+  const float2* table = reinterpret_cast<const float2*>(reinterpret_cast<const char*>(a.workspace) + kHeaderBytes);
   const int tid = threadIdx.x;
-  const uint32_t k0 = (uint32_t)a.seed;
-  const uint32_t k1 = (uint32_t)(a.seed >> 32);
-  constexpr float kMargin = 1.0f + 0x1p-21f;
 
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&ws->ticket, 1);
+    if (tid == 0) s_item = atomicAdd(&hdr->ticket, 1);
     __syncthreads();
     const int it = s_item;
     if (it >= a.n_items) break;
@@ -134,102 +333,31 @@ __global__ void __launch_bounds__(BLOCK) kb_f32(const mcl_b_args a) {
     }
     zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
 
-    // ---- slot initialisation: r' -> w, filled bits ----------------------
     const float alpha = (float)st.alpha;
-    float w[EPT];
-    uint32_t slot[EPT];
-    uint32_t filled = 0;
+    SlotState<EPT> S;
+    S.filled = 0;
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int e = item.slot_begin + i * BLOCK + tid;
-      slot[i] = (uint32_t)e;
-      w[i] = 0.0f;
-      if (e < st.n_slots) {
-        const uint4 r = philox4x32_10(0u, (uint32_t)e, st.set_id, kTagInit, k0, k1);
-        const float u = (float)(r.x >> 8) * 0x1p-24f;
-        w[i] = expf(-alpha * r_prime_f(u));
-        if (e < st.n_filled) filled |= 1u << i;
+      S.slot[i] = (uint32_t)e;
+      S.w[i] = 0.0f;
+      if (e < st.n_filled) {
+        const uint4 r0 = philox_ks(0u, (uint32_t)e, st.set_id, kTagInit, P);
+        S.w[i] = refill_w(r0.x, alpha);
+        S.filled |= 1u << i;
       }
     }
-    float weff[EPT];  // w of a filled trap, 0 for an empty one
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) weff[i] = (filled >> i & 1u) ? w[i] : 0.0f;
 
-    uint32_t cnt = 0;
     int64_t kglob = 0;  // global step of the set (fates, refill counters)
-    uint32_t qbase = 0;
+    uint32_t bbase = 0;  // Philox blocks used by earlier segments
+    const float2* tab = table + st.step_offset;
     for (int g = 0; g < st.seg_count; ++g) {
       const mcl_segment sg = a.segs[st.seg_begin + g];
-      const bool fill_on = sg.fill_rate > 0.0;
-      const int spb = sg.steps_per_bin;
-      int to_flush = spb;
-      int bin = sg.bin_offset;
-      for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
-        const int nj = min(kChunk, sg.n_steps - j0);
-        __syncthreads();
-        for (int jj = tid; jj < nj; jj += BLOCK) {
-          double c, q;
-          step_constants(st, sg, j0 + jj, c, q);
-          s_c[jj] = (float)c;
-          s_q[jj] = (float)q;
-        }
-        __syncthreads();
-        for (int jq = 0; jq < nj; jq += 4) {
-          const uint32_t quad = qbase + (uint32_t)((j0 + jq) >> 2);
-          uint4 r[EPT];
-#pragma unroll
-          for (int i = 0; i < EPT; ++i) r[i] = philox4x32_10(quad, slot[i], st.set_id, kTagStep, k0, k1);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (jq + q < nj) {
-              const float c = s_c[jq + q];
-              const float qf = s_q[jq + q];
-#pragma unroll
-              for (int i = 0; i < EPT; ++i) {
-                const uint32_t wd = word_of(r[i], q);
-                const float f = __uint_as_float((wd & 0x7fffffu) | 0x3f800000u);
-                const bool is_filled = (filled >> i) & 1u;
-                float y = __fmaf_rn(c, weff[i], kMargin);
-                if (fill_on && !is_filled) y = __fadd_rn(qf, kMargin);
-                if (f < y) {
-                  // exact test on the full 32-bit uniform (rotated left 9)
-                  const uint32_t u32 = __funnelshift_l(wd, wd, 9);
-                  if (is_filled) {
-                    const float p = -expm1f(-__fmul_rn(c, w[i]));
-                    if (p >= 1.0f || u32 < __float2uint_ru(__fmul_rn(p, 4294967296.0f))) {
-                      filled &= ~(1u << i);
-                      weff[i] = 0.0f;
-                      ++cnt;
-                      if (a.fates) a.fates[st.slot_offset + slot[i]] = (int32_t)(kglob + j0 + jq + q);
-                    }
-                  } else if (fill_on && slot[i] < (uint32_t)st.n_slots) {
-                    if (qf >= 1.0f || u32 < __float2uint_ru(__fmul_rn(qf, 4294967296.0f))) {
-                      const uint4 rr = philox4x32_10((uint32_t)(kglob + j0 + jq + q), slot[i],
-                                                     st.set_id, kTagRefill, k0, k1);
-                      const float u = (float)(rr.x >> 8) * 0x1p-24f;
-                      w[i] = expf(-alpha * r_prime_f(u));
-                      weff[i] = w[i];
-                      filled |= 1u << i;
-                    }
-                  }
-                }
-              }
-              if (--to_flush == 0 || j0 + jq + q + 1 == sg.n_steps) {
-                if (bin < st.n_bins) {
-                  warp_flush(cnt, &s_lum[bin]);
-                  if (s_alive) warp_flush((uint32_t)__popc(filled), &s_alive[bin]);
-                } else {
-                  report(a.status, MCL_ECAPACITY);
-                }
-                cnt = 0;
-                ++bin;
-                to_flush = spb;
-              }
-            }
-          }
-        }
-      }
-      qbase += (uint32_t)((sg.n_steps + 3) >> 2);
+      if (sg.fill_rate > 0.0)
+        segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
+      else
+        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
+      bbase += (uint32_t)((sg.n_steps + 7) >> 3);
       kglob += sg.n_steps;
     }
     __syncthreads();
@@ -242,21 +370,21 @@ __global__ void __launch_bounds__(BLOCK) kb_f32(const mcl_b_args a) {
 // FP64 kernel (Philox or injected uniforms): the oracle-parity mode
 // ---------------------------------------------------------------------------
 template <int BLOCK, int EPT, bool INJ>
-__global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
+__global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const mcl_b_args& a = P.a;
   double* s_c = reinterpret_cast<double*>(smem);
   double* s_q = s_c + kChunk;
   uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
   uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
   __shared__ int s_item;
 
-  Workspace* ws = reinterpret_cast<Workspace*>(a.workspace);
+  Header* hdr = reinterpret_cast<Header*>(a.workspace);
+  const double2* table = reinterpret_cast<const double2*>(reinterpret_cast<const char*>(a.workspace) + kHeaderBytes);
   const int tid = threadIdx.x;
-  const uint32_t k0 = (uint32_t)a.seed;
-  const uint32_t k1 = (uint32_t)(a.seed >> 32);
 
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&ws->ticket, 1);
+    if (tid == 0) s_item = atomicAdd(&hdr->ticket, 1);
     __syncthreads();
     const int it = s_item;
     if (it >= a.n_items) break;
@@ -283,7 +411,7 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
         if (INJ) {
           u = a.uniforms[st.u_offset + e];
         } else {
-          const uint4 r = philox4x32_10(0u, (uint32_t)e, st.set_id, kTagInit, k0, k1);
+          const uint4 r = philox_ks(0u, (uint32_t)e, st.set_id, kTagInit, P);
           u = u53(r.x, r.y);
         }
         w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u)));
@@ -291,19 +419,23 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
       }
     }
 
-    uint32_t cnt = 0;
     int64_t kglob = 0;
     uint32_t pbase = 0;
+    const double2* tab = table + st.step_offset;
     for (int g = 0; g < st.seg_count; ++g) {
       const mcl_segment sg = a.segs[st.seg_begin + g];
       const bool fill_on = sg.fill_rate > 0.0;
       const int spb = sg.steps_per_bin;
-      int to_flush = spb;
+      int to_flush = min(spb, sg.n_steps);
       int bin = sg.bin_offset;
       for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
         const int nj = min(kChunk, sg.n_steps - j0);
         __syncthreads();
-        for (int jj = tid; jj < nj; jj += BLOCK) step_constants(st, sg, j0 + jj, s_c[jj], s_q[jj]);
+        for (int jj = tid; jj < nj; jj += BLOCK) {
+          const double2 cq = tab[kglob + j0 + jj];
+          s_c[jj] = cq.x;
+          s_q[jj] = cq.y;
+        }
         __syncthreads();
         uint4 r[EPT];
         for (int jj = 0; jj < nj; ++jj) {
@@ -312,7 +444,7 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
           if (!INJ && (j & 1) == 0) {
 #pragma unroll
             for (int i = 0; i < EPT; ++i)
-              r[i] = philox4x32_10(pbase + (uint32_t)(j >> 1), slot[i], st.set_id, kTagStep, k0, k1);
+              r[i] = philox_ks(pbase + (uint32_t)(j >> 1), slot[i], st.set_id, kTagStep, P);
           }
           const double c = s_c[jj];
           const double qv = s_q[jj];
@@ -329,31 +461,19 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
               const double p = -expm1(__dmul_rn(-c, w[i]));
               if (u < p) {
                 filled &= ~(1u << i);
-                ++cnt;
+                atomicAdd(&s_lum[bin], 1u);
                 if (a.fates) a.fates[st.slot_offset + slot[i]] = (int32_t)k;
               }
-            } else if (fill_on && u < qv) {
-              double ur;
-              if (INJ) {
-                ur = 0.0;  // host validation rejects fill segments in injected mode
-              } else {
-                const uint4 rr = philox4x32_10((uint32_t)k, slot[i], st.set_id, kTagRefill, k0, k1);
-                ur = u53(rr.x, rr.y);
-              }
-              w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(ur)));
+            } else if (!INJ && fill_on && u < qv) {
+              const uint4 rr = philox_ks((uint32_t)k, slot[i], st.set_id, kTagRefill, P);
+              w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u53(rr.x, rr.y))));
               filled |= 1u << i;
             }
           }
-          if (--to_flush == 0 || j + 1 == sg.n_steps) {
-            if (bin < st.n_bins) {
-              warp_flush(cnt, &s_lum[bin]);
-              if (s_alive) warp_flush((uint32_t)__popc(filled), &s_alive[bin]);
-            } else {
-              report(a.status, MCL_ECAPACITY);
-            }
-            cnt = 0;
+          if (--to_flush == 0) {
+            if (s_alive) warp_flush((uint32_t)__popc(filled), &s_alive[bin]);
             ++bin;
-            to_flush = spb;
+            to_flush = min(spb, sg.n_steps - j - 1);
           }
         }
       }
@@ -366,12 +486,11 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const mcl_b_args a) {
   }
 }
 
-using KernelFn = void (*)(const mcl_b_args);
+using KernelFn = void (*)(const KParams);
 
 template <int BLOCK>
 KernelFn pick_f32(int ept) {
   switch (ept) {
-    case 1: return kb_f32<BLOCK, 1>;
     case 2: return kb_f32<BLOCK, 2>;
     case 4: return kb_f32<BLOCK, 4>;
     case 8: return kb_f32<BLOCK, 8>;
@@ -385,7 +504,6 @@ KernelFn pick_kernel(const mcl_b_args& a) {
     switch (a.block) {
       case 128: return pick_f32<128>(a.ept);
       case 256: return pick_f32<256>(a.ept);
-      case 512: return pick_f32<512>(a.ept);
     }
     return nullptr;
   }
@@ -401,12 +519,18 @@ KernelFn pick_kernel(const mcl_b_args& a) {
   return nullptr;
 }
 
+size_t table_entry_bytes(int32_t precision) { return precision == MCL_FP64 ? 16 : 8; }
+
 }  // namespace
 }  // namespace mcl
 
 using namespace mcl;
 
-extern "C" size_t mcl_b_workspace_size(void) { return sizeof(Workspace); }
+extern "C" size_t mcl_b_workspace_size(const mcl_set* sets, int32_t n_sets, int32_t precision) {
+  int64_t steps = 0;
+  for (int32_t i = 0; sets && i < n_sets; ++i) steps += sets[i].total_steps;
+  return (size_t)kHeaderBytes + (size_t)steps * table_entry_bytes(precision);
+}
 
 extern "C" size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t want_alive) {
   const size_t chunk = (precision == MCL_FP64 ? 2 * sizeof(double) : 2 * sizeof(float)) * kChunk;
@@ -416,7 +540,11 @@ extern "C" size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t 
 extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
   if (!args) return MCL_EINVAL;
   const mcl_b_args& a = *args;
-  if (a.n_items < 0 || a.max_bins < 0 || !a.workspace || !a.lum || !a.status) return MCL_EINVAL;
+  if (a.n_items < 0 || a.n_sets < 0 || a.max_bins < 0 || !a.workspace || !a.lum || !a.status)
+    return MCL_EINVAL;
+  if (a.table_steps < 0 ||
+      a.workspace_bytes < (int64_t)kHeaderBytes + a.table_steps * (int64_t)table_entry_bytes(a.precision))
+    return MCL_ECAPACITY;
   if (a.slots_per_item != a.block * a.ept) return MCL_EINVAL;
   if (a.rng == MCL_RNG_INJECTED && !a.uniforms) return MCL_EINVAL;
   KernelFn fn = pick_kernel(a);
@@ -424,6 +552,13 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const size_t smem = mcl_b_smem_bytes(a.max_bins, a.precision, a.alive != nullptr);
   if (smem > 200 * 1024) return MCL_ECAPACITY;
+  KParams P;
+  P.a = a;
+  const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    P.ks0[r] = k0 + (uint32_t)r * kPhiloxW0;
+    P.ks1[r] = k1 + (uint32_t)r * kPhiloxW1;
+  }
   MCL_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (a.zero_outputs) {
     MCL_CUDA_TRY(cudaMemsetAsync(a.lum, 0, sizeof(uint32_t) * (size_t)a.n_bins_total, s));
@@ -431,7 +566,14 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
     if (a.fates) MCL_CUDA_TRY(cudaMemsetAsync(a.fates, 0xff, sizeof(int32_t) * (size_t)a.n_slots_total, s));
     MCL_CUDA_TRY(cudaMemsetAsync(a.status, 0, sizeof(int32_t), s));
   }
-  MCL_CUDA_TRY(cudaMemsetAsync(a.workspace, 0, sizeof(Workspace), s));
+  MCL_CUDA_TRY(cudaMemsetAsync(a.workspace, 0, sizeof(Header), s));
+  if (a.n_sets > 0) {
+    if (a.precision == MCL_FP64)
+      kb_tables<double><<<a.n_sets, 256, 0, s>>>(a);
+    else
+      kb_tables<float><<<a.n_sets, 256, 0, s>>>(a);
+    MCL_CUDA_TRY(cudaGetLastError());
+  }
   if (a.n_items == 0) return MCL_OK;
   int grid = a.grid;
   if (grid <= 0) {
@@ -442,7 +584,7 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
     grid = sms * std::max(per_sm, 1);
   }
   grid = std::min(grid, a.n_items);
-  fn<<<grid, a.block, smem, s>>>(a);
+  fn<<<grid, a.block, smem, s>>>(P);
   MCL_CUDA_TRY(cudaGetLastError());
   return MCL_OK;
 }

@@ -34,10 +34,14 @@ segments, local step j of segment g of slot e draws from
 ``layout="f64"``      Philox4x32-10, two 53-bit doubles per call: words
                       (2(j&1), 2(j&1)+1) of philox(P_g + (j>>1), e, set_id,
                       TAG_STEP), P_g = sum of ceil(n_steps/2); FP64 mode.
-``layout="f32"``      Philox4x32-10, four 32-bit uniforms per call: word j&3 of
-                      philox(P_g + (j>>2), e, set_id, TAG_STEP), P_g = sum of
-                      ceil(n_steps/4), rotated left by 9 bits; an event happens
-                      iff u32 < p * 2^32.  The
+``layout="f32"``      Philox4x32-10, eight steps per call: step j takes the
+                      16-bit field h = bits 22..7 of word t&3 of
+                      philox(P_g + (j>>3), e, set_id, TAG_STEP), t = j&7,
+                      P_g = sum of ceil(n_steps/8); for t >= 4 the word's two
+                      16-bit halves are swapped first.  The uniform is
+                      u32 = (h << 16) | lo16 with lo16 the low 16 bits of word
+                      0 of philox(k, e, set_id, TAG_LOW) (k = the set's global
+                      step); an event happens iff u32 < p * 2^32.  The
                       kernel's FP32 mode draws the same integers, so its fates
                       agree with this FP64 evaluation except where p itself
                       differs in the last float bit (expected flips ~1e-6 per
@@ -51,7 +55,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .philox import TAG_INIT, TAG_REFILL, TAG_STEP, philox4x32, rotl9, seed_key, u53
+from .philox import TAG_INIT, TAG_LOW, TAG_REFILL, TAG_STEP, philox4x32, seed_key, u53
 
 K_B = 8.617333262145e-5
 
@@ -126,12 +130,14 @@ class _Draws:
         if self.layout == "f64":
             return (n_steps + 1) // 2
         if self.layout == "f32":
-            return (n_steps + 3) // 4
+            return (n_steps + 7) // 8
         return 0
 
-    def step(self, base, j, k):
+    def step(self, base, j, k, thr=None):
         """Uniforms of local step j (global step k) of the segment whose
-        Philox blocks start at ``base``, as doubles (f32: exact u32 / 2^32)."""
+        Philox blocks start at ``base``, as doubles.  In the f32 layout the
+        low 16 bits are drawn only where the high field lies below the
+        per-slot threshold ``thr`` (elsewhere u = h / 2^16 already decides)."""
         if self.layout == "f64":
             b = base + (j >> 1)
             if b != self._blk_id:
@@ -140,11 +146,22 @@ class _Draws:
             h = 2 * (j & 1)
             return u53(self._blk[h], self._blk[h + 1])
         if self.layout == "f32":
-            b = base + (j >> 2)
+            b = base + (j >> 3)
             if b != self._blk_id:
                 self._blk = philox4x32(b, self.e, self.sid, TAG_STEP, *self.key)
                 self._blk_id = b
-            return rotl9(self._blk[j & 3]).astype(np.float64) * 2.0 ** -32
+            t = j & 7
+            word = self._blk[t & 3]
+            if t >= 4:
+                word = ((word << np.uint64(16)) | (word >> np.uint64(16))) & np.uint64(0xFFFFFFFF)
+            h = (word >> np.uint64(7)) & np.uint64(0xFFFF)
+            u = h.astype(np.float64) * 2.0 ** -16
+            cand = np.nonzero(u < thr)[0]
+            if cand.size:
+                lo = philox4x32(k, cand.astype(np.uint64), self.sid, TAG_LOW, *self.key)[0]
+                u32 = (h[cand] << np.uint64(16)) | (lo & np.uint64(0xFFFF))
+                u[cand] = u32.astype(np.float64) * 2.0 ** -32
+            return u
         if self.layout == "injected":
             o = self.n + k * self.n
             return np.asarray(self.u[o:o + self.n], dtype=np.float64)
@@ -177,8 +194,8 @@ def run_set(st: dict, *, layout: str = "f64", seed: int = 0, uniforms=None,
         b0 = int(seg["bin_offset"])
         fill_on = float(seg.get("fill_rate", 0.0)) > 0
         for j in range(int(seg["n_steps"])):
-            u = dr.step(base, j, k)
             p = -np.expm1(-c[j] * w)
+            u = dr.step(base, j, k, np.where(filled, p, q[j]) if layout == "f32" else None)
             rec = filled & (u < p)
             b = b0 + j // spb
             nrec = int(np.count_nonzero(rec))

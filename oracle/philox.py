@@ -24,6 +24,7 @@ S32 = np.uint64(32)
 TAG_STEP = 0      # per-step Bernoulli uniforms
 TAG_INIT = 1      # initial nearest-centre distance r'
 TAG_REFILL = 2    # r' of a trap refilled at a given step
+TAG_LOW = 3       # low 16 bits of an FP32-layout uniform
 
 
 def philox4x32(c0, c1, c2, c3, k0, k1, rounds: int = 10):
@@ -47,13 +48,6 @@ def philox4x32(c0, c1, c2, c3, k0, k1, rounds: int = 10):
 def seed_key(seed: int):
     seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     return seed & 0xFFFFFFFF, seed >> 32
-
-
-def rotl9(w: np.ndarray) -> np.ndarray:
-    """The FP32 layout's 32-bit uniform: the word rotated left by 9 bits, so
-    that the low 23 bits of the word are the uniform's top 23 bits."""
-    w = np.asarray(w, dtype=np.uint64)
-    return ((w << np.uint64(9)) | (w >> np.uint64(23))) & MASK
 
 
 def u53(a: np.ndarray, b: np.ndarray) -> np.ndarray:

@@ -82,7 +82,7 @@ def test_fp32_fates_match_fp64_oracle_on_same_stream():
     assert total_mism <= 2
 
 
-@pytest.mark.parametrize("block,ept", [(128, 1), (256, 2), (256, 8), (512, 4)])
+@pytest.mark.parametrize("block,ept", [(128, 2), (256, 2), (256, 8), (128, 8)])
 def test_fp32_launch_shape_invariance(block, ept):
     specs = mixed_specs()
     ref = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=256, ept=4)
@@ -115,11 +115,14 @@ def test_graph_replay_is_deterministic():
 def test_glow_curve_statistics(alpha):
     """The single-set TL shape (2,000 traps, E = 1.45 eV, s = 3.5e12 /s,
     0 -> 500 degC at 1 K/s, dt = 0.1 s, 1 degC bins), R independent replicas in
-    FP32 native-Philox mode, against the exact FP64 expected curve:
-    every bin with enough counts within 3 MC standard errors (at most 1 % of
-    such bins outside), integrated signal within 0.5 % and within 4 SE, and
-    the peak temperature within 0.5 % (K)."""
-    R = 1024 if alpha < 50 else 4096
+    FP32 native-Philox mode, against the exact FP64 expected curve: bins with
+    enough counts within 3 MC standard errors, allowing only as many bins
+    outside as a correct sampler exceeds with probability 1e-3 (binomial
+    quantile of the 0.27 % two-sided 3-sigma rate), the chi-square of those
+    bins within its 1e-3..1-1e-3 band, the integrated signal within 0.5 %
+    and 4 SE, and the peak temperature within 0.5 % (K)."""
+    from scipy import stats
+    R = 4096
     base = schedule.single_tl_set(alpha=alpha)
     specs = []
     for r in range(R):
@@ -135,17 +138,23 @@ def test_glow_curve_statistics(alpha):
     se = np.sqrt(N * p * (1 - p))
     big = exp > 25
     if big.any():
-        z = np.abs(tot[big] - exp[big]) / se[big]
-        assert np.mean(z > 3) <= 0.01, np.sort(z)[-5:]
+        z = (tot[big] - exp[big]) / se[big]
+        n = int(big.sum())
+        allowed = stats.binom.ppf(0.999, n, 2 * stats.norm.sf(3.0))
+        assert np.sum(np.abs(z) > 3) <= allowed, np.sort(np.abs(z))[-5:]
+        chi2 = float(np.sum(z ** 2))
+        assert stats.chi2.ppf(1e-3, n) < chi2 < stats.chi2.ppf(1 - 1e-3, n), chi2 / n
     P = exp.sum() / N
     se_tot = np.sqrt(N * P * (1 - P))
     assert abs(tot.sum() - exp.sum()) <= 4 * se_tot + 1
-    if exp.sum() > 1e4:
+    # 0.5 % on the integrated signal is only testable where 3 SE < 0.5 %
+    if exp.sum() > 4e5:
         assert abs(tot.sum() - exp.sum()) / exp.sum() < 0.005
-        # peak of the 5-bin smoothed curves; bin b covers (b, b+1] degC
-        k = np.ones(5) / 5
-        t_peak = np.argmax(np.convolve(tot, k, "same")) + 273.65
-        e_peak = np.argmax(np.convolve(exp, k, "same")) + 273.65
+        # peak of the curves after the reference's presentation smoothing
+        # (50 degC boxcar, src/class/plots.py:39-47); bins start at 0 degC
+        k = np.ones(50) / 50
+        t_peak = np.argmax(np.convolve(tot, k, "valid")) + 273.15
+        e_peak = np.argmax(np.convolve(exp, k, "valid")) + 273.15
         assert abs(t_peak - e_peak) / e_peak < 0.005
 
 

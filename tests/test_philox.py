@@ -1,7 +1,7 @@
 """Philox4x32-10 against the known-answer vectors of the Random123 paper."""
 import numpy as np
 
-from oracle.philox import philox4x32, rotl9, u53
+from oracle.philox import philox4x32, u53
 
 KAT = [
     ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
@@ -26,7 +26,5 @@ def test_philox_vectorised_matches_scalar():
 
 
 def test_uniform_maps():
-    assert int(rotl9(0x007FFFFF)) == 0xFFFFFE00
-    assert int(rotl9(0xFF800000)) == 0x000001FF
     assert u53(0, 0) == 0.0
     assert u53(0xFFFFFFFF, 0xFFFFFFFF) < 1.0
