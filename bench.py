@@ -233,7 +233,15 @@ def main():
 
     # ---- roofline of the dominant kernel ------------------------------------
     from mcluminescence_gb300 import roofline
-    roof = roofline.bernoulli_fp32(trials, ms / 1e3, clk.get("sm_mhz"))
+    # DRAM bytes per launch: ncu capture of the 512-set case (31.1 MB, almost
+    # all of it the per-step rate table, which grows with the number of sets)
+    # scaled by 4096/512 sets.
+    traffic = 31.08e6 * a.sets / 512
+    roof = roofline.bernoulli_fp32(trials, ms / 1e3, clk.get("sm_mhz"), traffic=traffic)
+    roof["hbm_frac_of_measured"] = (traffic / (ms / 1e3)) / 6778e9
+    blocks_per_s = roofline.measure_philox_peak()
+    roof["philox_peak_trials_per_s"] = 8 * blocks_per_s
+    roof["frac_of_philox_peak"] = (trials / (ms / 1e3)) / (8 * blocks_per_s)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,

@@ -161,6 +161,12 @@ size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t want_alive)
 /* Launch on `stream` (stream-ordered, no host synchronisation). */
 int mcl_b_run(const mcl_b_args* args, void* stream);
 
+/* Roofline microbenchmark (no reference counterpart): `grid` CTAs of 256
+ * threads each generate iters x 4 Philox4x32-10 blocks with the Bernoulli
+ * kernel's counter layout and write one folded word per thread to
+ * sink[grid*256].  Blocks/s of this kernel x 8 bounds FP32 trials/s. */
+int mcl_bench_philox(uint32_t* sink, int32_t grid, int32_t iters, uint64_t seed, void* stream);
+
 /* ---- CUDA graphs -------------------------------------------------------- */
 /* Capture mcl_b_run(args) (with its output clearing) into a graph. */
 int mcl_b_graph_create(const mcl_b_args* args, void* stream, void** graph_out);

@@ -588,3 +588,39 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
   MCL_CUDA_TRY(cudaGetLastError());
   return MCL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Roofline microbenchmark: Philox4x32-10 block generation alone, with the same
+// counter structure as the FP32 kernel (block index and set id warp-uniform,
+// four slots per thread), XOR-folded into one word per thread.  The rate it
+// reaches bounds the FP32 kernel, which consumes one block per 8 trials.
+// ---------------------------------------------------------------------------
+namespace mcl {
+namespace {
+__global__ void __launch_bounds__(256) philox_peak_kernel(const KParams P, int iters, uint32_t* sink) {
+  const uint32_t slot0 = blockIdx.x * 1024u + threadIdx.x;
+  uint32_t acc = 0;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint4 r = philox_ks((uint32_t)it, slot0 + 256u * i, blockIdx.x, kTagStep, P);
+      acc ^= r.x ^ r.y ^ r.z ^ r.w;
+    }
+  }
+  sink[blockIdx.x * 256 + threadIdx.x] = acc;
+}
+}  // namespace
+}  // namespace mcl
+
+extern "C" int mcl_bench_philox(uint32_t* sink, int32_t grid, int32_t iters, uint64_t seed, void* stream) {
+  if (!sink || grid <= 0 || iters <= 0) return MCL_EINVAL;
+  KParams P{};
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    P.ks0[r] = k0 + (uint32_t)r * kPhiloxW0;
+    P.ks1[r] = k1 + (uint32_t)r * kPhiloxW1;
+  }
+  philox_peak_kernel<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(P, iters, sink);
+  MCL_CUDA_TRY(cudaGetLastError());
+  return MCL_OK;
+}

@@ -1,16 +1,25 @@
 """Roofline arithmetic for the kinetics kernels.
 
-The Bernoulli kernel reads only descriptors and writes only bins, so it is not
-bound by HBM or by tensor cores but by SM instruction issue: every
-electron-step trial needs a quarter of a Philox4x32-10 block (10 rounds of two
-32x32->64 multiplies and two three-input XORs = 40 operations per 4 uniforms)
-plus the three-operation fast test (form f from the uniform's top bits, one
-FMA, one compare): 13 algorithmic operations per trial.  The issue peak is
-4 sub-partitions x 32 lanes x SM clock x SMs thread-operations per second.
+The Bernoulli kernel reads only descriptors and a per-step rate table (a few
+hundred MB at most, L2-resident per set) and writes only bins, so neither HBM
+nor tensor cores bound it: it is bound by SM instruction issue on the integer
+(ALU) and FMA-heavy pipes, which execute the Philox rounds.
+
+Two denominators are reported:
+
+* ``issue``: the algorithmic operation count per electron-step trial -- one
+  eighth of a Philox4x32-10 block (10 rounds of two 32x32->64 multiplies and
+  two 3-input XORs = 40 operations per block of 8 trials = 5) plus the
+  three-operation fast test (form f from the 16-bit field, one FADD, one
+  FFMA) = 8 -- against the issue peak of 4 sub-partitions x 32 lanes x SM
+  clock x SMs;
+* ``philox``: the measured rate of a kernel that only generates Philox blocks
+  in the same counter layout (``mcl_bench_philox``); eight trials per block
+  is the most this design can reach.
 """
 from __future__ import annotations
 
-OPS_PER_TRIAL_FP32 = 13
+OPS_PER_TRIAL_FP32 = 8
 SMS = 152
 LANES_PER_SM = 128
 
@@ -29,3 +38,26 @@ def bernoulli_fp32(trials: int, seconds: float, sm_mhz=None, traffic=None) -> di
             "peak_basis": f"{SMS} SMs x {LANES_PER_SM} lanes x {mhz:.0f} MHz "
                           "(median SM clock sampled during the timed region)"
                           if sm_mhz else "max SM clock 2070 MHz"}
+
+
+def measure_philox_peak(iters: int = 4096, reps: int = 3) -> float:
+    """Philox4x32-10 blocks per second on the current GPU (CUDA events)."""
+    import ctypes as C
+    import torch
+    from . import _lib
+    lib = _lib.load()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    grid = sms * 8
+    sink = torch.empty(grid * 256, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream()
+    _lib.check(lib.mcl_bench_philox(C.c_void_p(sink.data_ptr()), grid, 64, 1, C.c_void_p(s.cuda_stream)),
+               "mcl_bench_philox")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        _lib.check(lib.mcl_bench_philox(C.c_void_p(sink.data_ptr()), grid, iters, 1,
+                                        C.c_void_p(s.cuda_stream)), "mcl_bench_philox")
+    e1.record(s)
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / reps
+    return grid * 256 * 4 * iters / sec
