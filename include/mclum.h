@@ -161,6 +161,24 @@ size_t mcl_b_smem_bytes(int32_t max_bins, int32_t precision, int32_t want_alive)
 /* Launch on `stream` (stream-ordered, no host synchronisation). */
 int mcl_b_run(const mcl_b_args* args, void* stream);
 
+/* Size of the library's own scratch array used by mcl_b_run_static. */
+#define MCL_B_STATIC_SCRATCH_BYTES (16 * 1024 * 1024)
+
+/* mcl_b_run without a caller-provided workspace (no counterpart in the
+ * reference).  For callers that may not allocate device memory -- e.g. a host
+ * application or plugin framework that owns all GPU memory through its own
+ * pool and forbids cudaMalloc, which can stall on work already queued.  The
+ * caller passes inputs and outputs exactly as for mcl_b_run; args->workspace
+ * and workspace_bytes are ignored.  Scratch comes from a static device array
+ * of MCL_B_STATIC_SCRATCH_BYTES held by every GPU that loads the library, so
+ * table_steps may be at most (MCL_B_STATIC_SCRATCH_BYTES - 256) / 8 (FP32) or
+ * / 16 (FP64); larger batches return MCL_ECAPACITY without launching.  The
+ * first call on a device looks up the array's device address (once per
+ * device, with that device current) and should come before any stream
+ * capture.  Calls share the array: ones that overlap on the GPU race, so
+ * issue them on one stream.  Allocates nothing. */
+int mcl_b_run_static(const mcl_b_args* args, void* stream);
+
 /* Roofline microbenchmark (no reference counterpart): `grid` CTAs of 256
  * threads each generate iters x 4 Philox4x32-10 blocks with the Bernoulli
  * kernel's counter layout and write one folded word per thread to

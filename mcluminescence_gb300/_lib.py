@@ -86,6 +86,7 @@ def _declare(lib):
         "mcl_b_run": (C.c_int, [C.POINTER(BArgs), vp]),
         "mcl_b_graph_create": (C.c_int, [C.POINTER(BArgs), vp, C.POINTER(vp)]),
         "mcl_bench_philox": (C.c_int, [vp, i32, i32, u64, vp]),
+        "mcl_b_run_static": (C.c_int, [C.POINTER(BArgs), vp]),
         "mcl_graph_launch": (C.c_int, [vp, vp]),
         "mcl_graph_destroy": (C.c_int, [vp]),
     }
@@ -100,7 +101,7 @@ EXPORTS = (
     "mcl_abi_version", "mcl_status_string", "mcl_last_error", "mcl_struct_sizes",
     "mcl_device_info", "mcl_b_validate", "mcl_b_pack_items", "mcl_b_workspace_size",
     "mcl_b_smem_bytes", "mcl_b_run", "mcl_b_graph_create", "mcl_graph_launch",
-    "mcl_graph_destroy", "mcl_bench_philox",
+    "mcl_graph_destroy", "mcl_bench_philox", "mcl_b_run_static",
 )
 
 
