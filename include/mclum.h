@@ -42,12 +42,14 @@ extern "C" {
 #define MCL_ECUDA (-4)      /* a CUDA runtime call failed                    */
 #define MCL_ENODEV (-5)     /* no usable sm_103 device                        */
 #define MCL_ENOHOLE (-6)    /* a nearest-centre search over zero centres      */
+#define MCL_EOVERFLOW (-7)  /* more steps than rows in an output table        */
 
 /* ---- precision / RNG selectors ---------------------------------------- */
 #define MCL_FP32 0          /* FP32 arithmetic, 32-bit Philox uniforms        */
 #define MCL_FP64 1          /* FP64 arithmetic, 53-bit Philox uniforms        */
 #define MCL_RNG_PHILOX 0    /* counter-based Philox4x32-10 keyed by seed      */
 #define MCL_RNG_INJECTED 1  /* caller-supplied uniforms (FP64 only)           */
+#define MCL_RNG_MT19937 2   /* numpy's legacy RandomState stream (MT19937)    */
 
 /* ---- Bernoulli-mode schedule ------------------------------------------ */
 #define MCL_SEG_THERMAL 1   /* add s*exp(-E/(k_b*T)) to the segment's rate   */
@@ -131,13 +133,67 @@ typedef struct mcl_b_args {
   int32_t reserved;
 } mcl_b_args;
 
+/* ---- reference-kinetics (event-driven) mode ----------------------------- */
+/* One simulation: one (run, sim) pair of src/class/simulate.py:36-92, with
+ * the run's parameters already read the way simulate.py:39-45 and
+ * tl_trap_lab.py:27-43 read them (box sides computed on the host in FP64).  */
+typedef struct mcl_k_sim {
+  double alpha, b, s, E_cb, E_loc_1, E_loc_2, D0, Retrap, k_b;
+  double dose_rate;     /* simulate.py:42 reads physics_fp.dose_rate         */
+  double T_start;       /* degC                                               */
+  double T_rate;        /* K/s                                                */
+  double dt_cap;        /* max_dt / T_rate, or 1e20 when T_rate == 0          */
+  double duration;      /* s                                                  */
+  double N_e;           /* trap count (electron_ratio = n / N_e)              */
+  double L, W, H;       /* core box sides                                     */
+  double Lb, Wb, Hb;    /* boundary box sides (x boundary_factor)             */
+  int32_t e0;           /* initial electrons int(N_e * e_ratio_start)         */
+  int32_t n_h0;         /* initial holes int(holes * bf^3)                    */
+  int32_t e_cap;        /* electron capacity (e0 + pair creations allowed)   */
+  int32_t h_cap;        /* hole capacity                                      */
+  int32_t steps;        /* rows of the output tables                          */
+  uint32_t stream_id;   /* Philox stream of this simulation                   */
+  int64_t out_offset;   /* first row of this simulation in the tables         */
+  int64_t u_offset;     /* injected: first uniform (sequential mode: sim 0 only; */
+  int64_t u_count;      /*   later sims continue the stream); uniforms available */
+  int64_t ws_offset;    /* bytes into the workspace (arrays in global memory) */
+  int64_t ev_offset;    /* first event slot in events[] (4 int32 per event)   */
+  int64_t ev_cap;       /* event slots of this simulation                     */
+} mcl_k_sim;
+
+typedef struct mcl_k_args {
+  const mcl_k_sim* sims;
+  double* x_ax;            /* [rows] time after each step, zero padded        */
+  double* lum;             /* [rows] 1.0 on recombination steps               */
+  double* ratio;           /* [rows] electrons / N_e after each step          */
+  int32_t* events;         /* [4 * slots] step, kind(0 pair created, 1 recombination), e, h; or NULL */
+  int32_t* n_events;       /* [n_sims]                                         */
+  int32_t* n_steps;        /* [n_sims] steps taken                             */
+  int64_t* draws;          /* [n_sims] uniforms consumed                       */
+  int32_t* status;         /* [n_sims] 0 or a negative MCL_E* code            */
+  const double* uniforms;  /* MCL_RNG_INJECTED                                 */
+  uint32_t* mt_state;      /* MCL_RNG_MT19937: [625] key words + position, in/out */
+  void* workspace;         /* global-memory arrays when they exceed shared memory */
+  int64_t workspace_bytes;
+  uint64_t seed;           /* MCL_RNG_PHILOX key                               */
+  int32_t n_sims;
+  int32_t rng;
+  int32_t sequential;      /* 1: one CTA runs the simulations in order on one stream */
+  int32_t block;           /* 256 or 512                                       */
+  int32_t e_cap_max;       /* largest e_cap / h_cap (from mcl_k_validate)      */
+  int32_t h_cap_max;
+  int32_t arrays_in_smem;  /* 1: electron/hole arrays in shared memory (from mcl_k_validate) */
+  int32_t reserved;
+} mcl_k_args;
+
 /* ---- library ------------------------------------------------------------ */
 int mcl_abi_version(void);
 const char* mcl_status_string(int code);
 /* Text of the last CUDA error seen by this thread's calls ("" if none). */
 const char* mcl_last_error(void);
 /* sizeof(mcl_segment), sizeof(mcl_set), sizeof(mcl_item), sizeof(mcl_b_args),
- * written to out[0..3], so bindings can check their struct layouts. */
+ * sizeof(mcl_k_sim), sizeof(mcl_k_args), written to out[0..5], so bindings
+ * can check their struct layouts. */
 int mcl_struct_sizes(size_t* out);
 /* SM count and compute capability of the current device. */
 int mcl_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
@@ -184,6 +240,21 @@ int mcl_b_run_static(const mcl_b_args* args, void* stream);
  * kernel's counter layout and write one folded word per thread to
  * sink[grid*256].  Blocks/s of this kernel x 8 bounds FP32 trials/s. */
 int mcl_bench_philox(uint32_t* sink, int32_t grid, int32_t iters, uint64_t seed, void* stream);
+
+/* ---- reference-kinetics mode ----------------------------------------------- */
+/* Host validation; also reports whether the electron/hole arrays of the
+ * largest simulation fit in shared memory (*arrays_in_smem), the workspace
+ * bytes needed otherwise (*workspace_bytes; each simulation's arrays start at
+ * its ws_offset) and the largest capacities, all to be copied into
+ * mcl_k_args. */
+int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng, int32_t block,
+                   int64_t n_uniforms, int32_t* arrays_in_smem, int64_t* workspace_bytes,
+                   int32_t* e_cap_max, int32_t* h_cap_max);
+/* Launch (stream-ordered).  Per-simulation problems land in status[]:
+ * MCL_ECAPACITY when the output table is too short (the reference raises
+ * IndexError, simulate.py:64) or a capacity is exceeded, MCL_EBUDGET when an
+ * injected stream runs out, MCL_ENOHOLE for a nearest search over no holes. */
+int mcl_k_run(const mcl_k_args* args, void* stream);
 
 /* ---- CUDA graphs -------------------------------------------------------- */
 /* Capture mcl_b_run(args) (with its output clearing) into a graph. */

@@ -16,3 +16,6 @@ __all__ = [
     "irradiate", "fade", "optical", "single_tl_set", "batch_tl_iso", "batch_dose_fade_irsl",
     "BernoulliBatch", "BatchResult", "simulate_batch",
 ]
+from .kinetics import run_kinetics, run_params, simulate, write_table  # noqa: F401,E402
+
+__all__ += ["simulate", "run_kinetics", "run_params", "write_table"]

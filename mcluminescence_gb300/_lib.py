@@ -21,11 +21,13 @@ MCL_EBUDGET = -3
 MCL_ECUDA = -4
 MCL_ENODEV = -5
 MCL_ENOHOLE = -6
+MCL_EOVERFLOW = -7
 
 MCL_FP32 = 0
 MCL_FP64 = 1
 MCL_RNG_PHILOX = 0
 MCL_RNG_INJECTED = 1
+MCL_RNG_MT19937 = 2
 MCL_SEG_THERMAL = 1
 
 # numpy mirrors of the C structs (natural alignment, little endian)
@@ -51,6 +53,27 @@ class BArgs(C.Structure):
         ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
         ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
         ("zero_outputs", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+K_SIM_DTYPE = np.dtype(
+    [(n, "<f8") for n in ("alpha", "b", "s", "E_cb", "E_loc_1", "E_loc_2", "D0", "Retrap", "k_b",
+                          "dose_rate", "T_start", "T_rate", "dt_cap", "duration", "N_e",
+                          "L", "W", "H", "Lb", "Wb", "Hb")]
+    + [(n, "<i4") for n in ("e0", "n_h0", "e_cap", "h_cap", "steps")] + [("stream_id", "<u4")]
+    + [(n, "<i8") for n in ("out_offset", "u_offset", "u_count", "ws_offset", "ev_offset", "ev_cap")],
+    align=True)
+
+
+class KArgs(C.Structure):
+    _fields_ = [
+        ("sims", C.c_void_p), ("x_ax", C.c_void_p), ("lum", C.c_void_p), ("ratio", C.c_void_p),
+        ("events", C.c_void_p), ("n_events", C.c_void_p), ("n_steps", C.c_void_p),
+        ("draws", C.c_void_p), ("status", C.c_void_p), ("uniforms", C.c_void_p),
+        ("mt_state", C.c_void_p), ("workspace", C.c_void_p), ("workspace_bytes", C.c_int64),
+        ("seed", C.c_uint64), ("n_sims", C.c_int32), ("rng", C.c_int32), ("sequential", C.c_int32),
+        ("block", C.c_int32), ("e_cap_max", C.c_int32), ("h_cap_max", C.c_int32),
+        ("arrays_in_smem", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -87,6 +110,9 @@ def _declare(lib):
         "mcl_b_graph_create": (C.c_int, [C.POINTER(BArgs), vp, C.POINTER(vp)]),
         "mcl_bench_philox": (C.c_int, [vp, i32, i32, u64, vp]),
         "mcl_b_run_static": (C.c_int, [C.POINTER(BArgs), vp]),
+        "mcl_k_validate": (C.c_int, [vp, i32, i32, i32, i64, C.POINTER(i32), C.POINTER(i64),
+                                     C.POINTER(i32), C.POINTER(i32)]),
+        "mcl_k_run": (C.c_int, [C.POINTER(KArgs), vp]),
         "mcl_graph_launch": (C.c_int, [vp, vp]),
         "mcl_graph_destroy": (C.c_int, [vp]),
     }
@@ -101,7 +127,7 @@ EXPORTS = (
     "mcl_abi_version", "mcl_status_string", "mcl_last_error", "mcl_struct_sizes",
     "mcl_device_info", "mcl_b_validate", "mcl_b_pack_items", "mcl_b_workspace_size",
     "mcl_b_smem_bytes", "mcl_b_run", "mcl_b_graph_create", "mcl_graph_launch",
-    "mcl_graph_destroy", "mcl_bench_philox", "mcl_b_run_static",
+    "mcl_graph_destroy", "mcl_bench_philox", "mcl_b_run_static", "mcl_k_validate", "mcl_k_run",
 )
 
 
@@ -120,9 +146,10 @@ def load(auto_build: bool = False):
         lib = _declare(C.CDLL(path))
         if lib.mcl_abi_version() != 1:
             raise RuntimeError("libmclum ABI version mismatch; rebuild the library")
-        sizes = (C.c_size_t * 4)()
+        sizes = (C.c_size_t * 6)()
         lib.mcl_struct_sizes(sizes)
-        want = (SEG_DTYPE.itemsize, SET_DTYPE.itemsize, ITEM_DTYPE.itemsize, C.sizeof(BArgs))
+        want = (SEG_DTYPE.itemsize, SET_DTYPE.itemsize, ITEM_DTYPE.itemsize, C.sizeof(BArgs),
+                K_SIM_DTYPE.itemsize, C.sizeof(KArgs))
         if tuple(sizes) != want:
             raise RuntimeError(f"struct layout mismatch: library {tuple(sizes)} vs binding {want}")
         _LIB[0] = lib

@@ -31,6 +31,8 @@ extern "C" int mcl_struct_sizes(size_t* out) {
   out[1] = sizeof(mcl_set);
   out[2] = sizeof(mcl_item);
   out[3] = sizeof(mcl_b_args);
+  out[4] = sizeof(mcl_k_sim);
+  out[5] = sizeof(mcl_k_args);
   return MCL_OK;
 }
 
@@ -43,6 +45,7 @@ extern "C" const char* mcl_status_string(int code) {
     case MCL_ECUDA: return "CUDA runtime error";
     case MCL_ENODEV: return "no usable sm_103 device";
     case MCL_ENOHOLE: return "nearest-centre search over zero recombination centres";
+    case MCL_EOVERFLOW: return "more steps than rows in the output table";
   }
   return "unknown status";
 }

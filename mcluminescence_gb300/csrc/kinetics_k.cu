@@ -1,0 +1,663 @@
+// Event-driven (reference) trap kinetics: the loop of src/class/simulate.py:51-92
+// over TLTrapSim / Box / Physics (src/class/tl_trap_lab.py:27-60,
+// src/class/engine.py:65-188), one CTA per simulation, FP64.
+//
+// Per step, exactly as the reference:
+//   T = T_start + T_rate t + 273.15                        (simulate.py:53-54)
+//   per electron: E_loc = U < Retrap ? E_loc_2 : E_loc_1    (engine.py:72)
+//                 wait = 1/(s e^{-E_cb/kT} + b e^{-E_loc/kT - alpha d}) * -log(1-U)
+//                                                         (engine.py:65-77, tl_trap_lab.py:48-51)
+//   fill wait: lambda = (D/D0)(N-n), or 1e-20 when n == N or D == 0;
+//              one uniform whenever lambda > 0           (tl_trap_lab.py:53-60)
+//   dt = min(dt_fill, min wait (if any wait != 0, else dt_fill), dt_cap)
+//   one event: pair creation, recombination of the first electron with the
+//   minimal wait and its nearest hole, or nothing        (simulate.py:56-84)
+// with the reference's bookkeeping quirks (engine.py:133-175): a created
+// electron searches the OLD holes only, existing electrons are not re-pointed
+// to the new hole, and after a removal the hole indices above the removed one
+// shift down BEFORE the electrons pointing at the removed index are rescanned
+// (so the former h+1 owners are rescanned too).  Arrays are shifted like
+// np.delete, so every index the kernel reports is the reference's index.
+//
+// Uniforms are consumed in the reference's order (engine.py:125,128; then per
+// step engine.py:72, tl_trap_lab.py:51, :60, and engine.py:135-136 on a pair
+// creation) from one of three sources:
+//   MT19937   numpy's legacy RandomState stream, generated in shared memory
+//             (the key array and position come from / go back to the host,
+//             so np.random.seed(k); simulate(cfg) is reproduced draw by draw);
+//   injected  a caller-provided array of doubles;
+//   Philox    an independent counter-based stream per simulation.
+// Distances follow np.linalg.norm's order sqrt((dx*dx + dy*dy) + dz*dz) with no
+// contraction; nearest searches compare squared distances and take the square
+// root only when it can decide (first index wins ties, like np.argmin).
+#include <climits>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mcl {
+namespace {
+
+constexpr int kRing = 4096;          // MT19937 output ring (words), power of two
+constexpr int kChunk = 1024;         // doubles consumed per chunk
+constexpr uint32_t kTagK = 4;        // Philox tag of the event-driven draws
+constexpr int kMtN = 624;
+constexpr int kMtM = 397;
+
+static_assert(2 * kChunk + 2 * kMtN <= kRing, "ring too small for a chunk");
+
+__device__ __forceinline__ double dsq3(double ax, double ay, double az, double bx, double by, double bz) {
+  const double dx = __dadd_rn(ax, -bx);
+  const double dy = __dadd_rn(ay, -by);
+  const double dz = __dadd_rn(az, -bz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// (v2, i2) beats (v1, i1) under np.argmin: NaN first, then smaller, then lower index.
+__device__ __forceinline__ bool better(double v2, int i2, double v1, int i1) {
+  const bool n1 = isnan(v1), n2 = isnan(v2);
+  if (n2 != n1) return n2;
+  if (n1) return i2 < i1;
+  return v2 < v1 || (v2 == v1 && i2 < i1);
+}
+
+struct Arrays {
+  double *ex, *ey, *ez, *ed;  // electron coordinates, nearest distance
+  int32_t* en;                // nearest hole index
+  uint8_t* choice;            // E_loc choice of the current step
+  int32_t* mlist;             // electrons to rescan after a removal
+  double *hx, *hy, *hz;       // hole coordinates
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t arrays_bytes(int e_cap, int h_cap) {
+  return align16(sizeof(double) * 4 * (size_t)e_cap) + align16(sizeof(int32_t) * (size_t)e_cap) +
+         align16((size_t)e_cap) + align16(sizeof(int32_t) * (size_t)e_cap) +
+         align16(sizeof(double) * 3 * (size_t)h_cap);
+}
+
+__device__ inline Arrays carve(unsigned char* base, int e_cap, int h_cap) {
+  Arrays A;
+  double* d = reinterpret_cast<double*>(base);
+  A.ex = d;
+  A.ey = d + e_cap;
+  A.ez = d + 2 * e_cap;
+  A.ed = d + 3 * e_cap;
+  unsigned char* p = base + align16(sizeof(double) * 4 * (size_t)e_cap);
+  A.en = reinterpret_cast<int32_t*>(p);
+  p += align16(sizeof(int32_t) * (size_t)e_cap);
+  A.choice = p;
+  p += align16((size_t)e_cap);
+  A.mlist = reinterpret_cast<int32_t*>(p);
+  p += align16(sizeof(int32_t) * (size_t)e_cap);
+  double* h = reinterpret_cast<double*>(p);
+  A.hx = h;
+  A.hy = h + h_cap;
+  A.hz = h + 2 * h_cap;
+  return A;
+}
+
+// Shared scalars of the CTA.
+struct Shared {
+  double rv[32];
+  int ri[32];
+  int ra[32];
+  double best_v;
+  int best_i;
+  int any;
+  int n_mask;
+};
+
+// Block-wide argmin with np.argmin semantics; also ORs `any`.
+template <int BLOCK>
+__device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v, int& out_i, int& out_any) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_down_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_down_sync(0xffffffffu, i, o);
+    const int a2 = __shfl_down_sync(0xffffffffu, any, o);
+    if (better(v2, i2, v, i)) {
+      v = v2;
+      i = i2;
+    }
+    any |= a2;
+  }
+  if (lane == 0) {
+    sh.rv[warp] = v;
+    sh.ri[warp] = i;
+    sh.ra[warp] = any;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int W = BLOCK / 32;
+    v = lane < W ? sh.rv[lane] : INFINITY;
+    i = lane < W ? sh.ri[lane] : INT_MAX;
+    any = lane < W ? sh.ra[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_down_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_down_sync(0xffffffffu, i, o);
+      const int a2 = __shfl_down_sync(0xffffffffu, any, o);
+      if (better(v2, i2, v, i)) {
+        v = v2;
+        i = i2;
+      }
+      any |= a2;
+    }
+    if (lane == 0) {
+      sh.best_v = v;
+      sh.best_i = i;
+      sh.any = any;
+    }
+  }
+  __syncthreads();
+  out_v = sh.best_v;
+  out_i = sh.best_i;
+  out_any = sh.any;
+  __syncthreads();
+}
+
+// Nearest hole of point p over holes [0, n_h): exact np.argmin of the norms.
+// Per thread: running best over its strided holes; sqrt only when the squared
+// distance does not exceed the best squared distance so far.
+template <int BLOCK>
+__device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, double py, double pz,
+                              double& d_out, int& i_out) {
+  double bsq = INFINITY, bd = INFINITY;
+  int bi = INT_MAX;
+  for (int h = threadIdx.x; h < n_h; h += BLOCK) {
+    const double sq = dsq3(px, py, pz, A.hx[h], A.hy[h], A.hz[h]);
+    if (sq <= bsq) {
+      const double d = __dsqrt_rn(sq);
+      if (d < bd) {
+        bd = d;
+        bsq = sq;
+        bi = h;
+      }
+    }
+  }
+  int dummy;
+  block_argmin<BLOCK>(sh, bd, bi, 0, d_out, i_out, dummy);
+}
+
+// ---------------------------------------------------------------------------
+// Uniform sources
+// ---------------------------------------------------------------------------
+struct Source {
+  int rng;
+  // injected
+  const double* u;
+  int64_t u_base, u_count;
+  // Philox
+  uint32_t k0, k1, stream;
+  // MT19937 (shared memory)
+  uint32_t* mt;    // 624 key words
+  uint32_t* ring;  // kRing tempered words
+  uint32_t rd, wr;  // ring positions (identical in every thread)
+  int64_t pos;     // doubles consumed in this simulation
+};
+
+__device__ __forceinline__ uint32_t mt_mix(uint32_t xi, uint32_t xi1, uint32_t xm) {
+  const uint32_t y = (xi & 0x80000000u) | (xi1 & 0x7fffffffu);
+  return xm ^ (y >> 1) ^ ((xi1 & 1u) ? 0x9908b0dfu : 0u);
+}
+
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+
+// One MT19937 state transition (Matsumoto & Nishimura 1998) by the whole CTA:
+// indices [0,227) read only old words, [227,454) and [454,623) read words
+// updated 227 places earlier, 623 reads the new words 0 and 396.
+template <int BLOCK>
+__device__ void mt_twist(uint32_t* mt) {
+  const int t = threadIdx.x;
+  uint32_t v = 0;
+  if (t < kMtN - kMtM) v = mt_mix(mt[t], mt[t + 1], mt[t + kMtM]);
+  __syncthreads();
+  if (t < kMtN - kMtM) mt[t] = v;
+  __syncthreads();
+  const int i1 = t + (kMtN - kMtM);
+  if (i1 < 2 * (kMtN - kMtM)) v = mt_mix(mt[i1], mt[i1 + 1], mt[i1 - (kMtN - kMtM)]);
+  __syncthreads();
+  if (i1 < 2 * (kMtN - kMtM)) mt[i1] = v;
+  __syncthreads();
+  const int i2 = t + 2 * (kMtN - kMtM);
+  if (i2 < kMtN - 1) v = mt_mix(mt[i2], mt[i2 + 1], mt[i2 - (kMtN - kMtM)]);
+  __syncthreads();
+  if (i2 < kMtN - 1) mt[i2] = v;
+  __syncthreads();
+  if (t == 0) mt[kMtN - 1] = mt_mix(mt[kMtN - 1], mt[0], mt[kMtM - 1]);
+  __syncthreads();
+}
+
+// Make `n` doubles available (n <= kChunk).  Returns false when an injected
+// stream would run out.
+template <int BLOCK>
+__device__ bool ensure(Source& S, int n) {
+  if (S.rng == MCL_RNG_INJECTED) return S.pos + n <= S.u_count;
+  if (S.rng != MCL_RNG_MT19937) return true;
+  while ((int)(S.wr - S.rd) < 2 * n) {
+    mt_twist<BLOCK>(S.mt);
+    for (int k = threadIdx.x; k < kMtN; k += BLOCK) S.ring[(S.wr + k) & (kRing - 1)] = mt_temper(S.mt[k]);
+    S.wr += kMtN;
+    __syncthreads();
+  }
+  return true;
+}
+
+__device__ __forceinline__ double value(const Source& S, int k) {
+  if (S.rng == MCL_RNG_MT19937) {
+    const uint32_t a = S.ring[(S.rd + 2u * k) & (kRing - 1)];
+    const uint32_t b = S.ring[(S.rd + 2u * k + 1u) & (kRing - 1)];
+    return u53(a, b);
+  }
+  if (S.rng == MCL_RNG_INJECTED) return S.u[S.u_base + S.pos + k];
+  const uint64_t d = (uint64_t)(S.pos + k);
+  const uint4 r = philox4x32_10((uint32_t)(d >> 1), S.stream, (uint32_t)(d >> 33), kTagK, S.k0, S.k1);
+  return (d & 1) ? u53(r.z, r.w) : u53(r.x, r.y);
+}
+
+__device__ __forceinline__ void advance(Source& S, int n) {
+  S.pos += n;
+  if (S.rng == MCL_RNG_MT19937) S.rd += 2u * n;
+}
+
+// ---------------------------------------------------------------------------
+// One simulation by the whole CTA
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const Arrays& A, Shared& sh,
+                       Source& S) {
+  const int tid = threadIdx.x;
+  int status = MCL_OK;
+  int n_e = sm.e0, n_h = sm.n_h0;
+  int n_ev = 0;
+  S.pos = 0;
+
+  // ---- seeding (engine.py:124-129): electrons, then holes -----------------
+  if (n_e > sm.e_cap || n_h > sm.h_cap) status = MCL_ECAPACITY;
+  for (int pass = 0; pass < 2 && status == MCL_OK; ++pass) {
+    const int cnt_all = 3 * (pass == 0 ? n_e : n_h);
+    double* X = pass == 0 ? A.ex : A.hx;
+    double* Y = pass == 0 ? A.ey : A.hy;
+    double* Z = pass == 0 ? A.ez : A.hz;
+    const double sx = pass == 0 ? sm.L : sm.Lb, sy = pass == 0 ? sm.W : sm.Wb, sz = pass == 0 ? sm.H : sm.Hb;
+    for (int c0 = 0; c0 < cnt_all; c0 += kChunk) {
+      const int cnt = min(kChunk, cnt_all - c0);
+      if (!ensure<BLOCK>(S, cnt)) {
+        status = MCL_EBUDGET;
+        break;
+      }
+      for (int k = tid; k < cnt; k += BLOCK) {
+        const int idx = c0 + k, p = idx / 3, c = idx - 3 * p;
+        const double u = value(S, k);
+        if (c == 0) X[p] = __dmul_rn(u, sx);
+        else if (c == 1) Y[p] = __dmul_rn(u, sy);
+        else Z[p] = __dmul_rn(u, sz);
+      }
+      advance(S, cnt);
+      __syncthreads();
+    }
+  }
+
+  // ---- full nearest search (engine.py:113-119) ----------------------------
+  if (status == MCL_OK) {
+    if (n_e > 0 && n_h == 0) status = MCL_ENOHOLE;
+    for (int e = tid; e < n_e && status == MCL_OK; e += BLOCK) {
+      const double px = A.ex[e], py = A.ey[e], pz = A.ez[e];
+      double bsq = INFINITY, bd = INFINITY;
+      int bi = INT_MAX;
+      for (int h = 0; h < n_h; ++h) {
+        const double sq = dsq3(px, py, pz, A.hx[h], A.hy[h], A.hz[h]);
+        if (sq <= bsq) {
+          const double d = __dsqrt_rn(sq);
+          if (d < bd) {
+            bd = d;
+            bsq = sq;
+            bi = h;
+          }
+        }
+      }
+      A.ed[e] = bd;
+      A.en[e] = bi;
+    }
+    __syncthreads();
+  }
+
+  // ---- the step loop (simulate.py:51-92) ---------------------------------
+  const int64_t N = (int64_t)sm.N_e;
+  double t = 0.0;
+  int i = 0;
+  const int64_t out = sm.out_offset;
+  while (status == MCL_OK && t <= sm.duration) {
+    const double T = __dadd_rn(__dadd_rn(sm.T_start, __dmul_rn(sm.T_rate, t)), 273.15);
+    const double kT = __dmul_rn(sm.k_b, T);
+    const double rcb = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT)));
+
+    // E_loc choices: n uniforms
+    for (int c0 = 0; c0 < n_e; c0 += kChunk) {
+      const int cnt = min(kChunk, n_e - c0);
+      if (!ensure<BLOCK>(S, cnt)) {
+        status = MCL_EBUDGET;
+        break;
+      }
+      for (int k = tid; k < cnt; k += BLOCK) A.choice[c0 + k] = value(S, k) < sm.Retrap ? 1 : 0;
+      advance(S, cnt);
+      __syncthreads();
+    }
+    if (status != MCL_OK) break;
+    // waits: n uniforms, argmin and any()
+    double bv = INFINITY;
+    int bi = INT_MAX, any = 0;
+    for (int c0 = 0; c0 < n_e; c0 += kChunk) {
+      const int cnt = min(kChunk, n_e - c0);
+      if (!ensure<BLOCK>(S, cnt)) {
+        status = MCL_EBUDGET;
+        break;
+      }
+      for (int k = tid; k < cnt; k += BLOCK) {
+        const int e = c0 + k;
+        const double E_loc = A.choice[e] ? sm.E_loc_2 : sm.E_loc_1;
+        const double arg = __dadd_rn(__ddiv_rn(-E_loc, kT), -__dmul_rn(sm.alpha, A.ed[e]));
+        const double rate = __dmul_rn(sm.b, exp(arg));
+        const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
+        const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -value(S, k))));
+        any |= (w != 0.0);
+        if (better(w, e, bv, bi)) {
+          bv = w;
+          bi = e;
+        }
+      }
+      advance(S, cnt);
+      __syncthreads();
+    }
+    if (status != MCL_OK) break;
+    double wmin;
+    int emin;
+    block_argmin<BLOCK>(sh, bv, bi, any, wmin, emin, any);
+
+    // filling wait (tl_trap_lab.py:53-60)
+    double lam;
+    if ((int64_t)n_e == N || sm.dose_rate == 0.0) lam = 1e-20;
+    else lam = __dmul_rn(__ddiv_rn(sm.dose_rate, sm.D0), (double)(N - (int64_t)n_e));
+    double dt_fill = 1e20;
+    if (lam > 0.0) {
+      if (!ensure<BLOCK>(S, 1)) {
+        status = MCL_EBUDGET;
+        break;
+      }
+      dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -value(S, 0))));
+      advance(S, 1);
+    }
+    const double dt_recomb = any ? wmin : dt_fill;
+    double dt = dt_fill;  // Python's min(): the first minimal argument
+    if (dt_recomb < dt) dt = dt_recomb;
+    if (sm.dt_cap < dt) dt = sm.dt_cap;
+    t = __dadd_rn(t, dt);
+    if (i >= sm.steps) {  // x_ax[i] would raise IndexError (simulate.py:64)
+      status = MCL_EOVERFLOW;
+      break;
+    }
+    if (tid == 0) a.x_ax[out + i] = t;
+    double ev = 0.0;
+
+    if (dt == dt_fill) {
+      // ---- pair creation (engine.py:133-152) ----
+      if (!ensure<BLOCK>(S, 6)) {
+        status = MCL_EBUDGET;
+        break;
+      }
+      const double nex = __dmul_rn(value(S, 0), sm.L), ney = __dmul_rn(value(S, 1), sm.W),
+                   nez = __dmul_rn(value(S, 2), sm.H);
+      const double nhx = __dmul_rn(value(S, 3), sm.Lb), nhy = __dmul_rn(value(S, 4), sm.Wb),
+                   nhz = __dmul_rn(value(S, 5), sm.Hb);
+      advance(S, 6);
+      if (n_h == 0) {
+        status = MCL_ENOHOLE;
+        break;
+      }
+      if (n_e + 1 > sm.e_cap || n_h + 1 > sm.h_cap) {
+        status = MCL_ECAPACITY;
+        break;
+      }
+      double dn;
+      int hn;
+      nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, dn, hn);  // OLD holes only
+      if (tid == 0) {
+        A.ex[n_e] = nex;
+        A.ey[n_e] = ney;
+        A.ez[n_e] = nez;
+        A.ed[n_e] = dn;
+        A.en[n_e] = hn;
+        A.hx[n_h] = nhx;
+        A.hy[n_h] = nhy;
+        A.hz[n_h] = nhz;
+        if (a.events && n_ev < sm.ev_cap) {
+          int32_t* evp = a.events + 4 * (sm.ev_offset + n_ev);
+          evp[0] = i;
+          evp[1] = 0;
+          evp[2] = n_e;
+          evp[3] = n_h;
+        }
+      }
+      ++n_e;
+      ++n_h;
+      ++n_ev;
+      __syncthreads();
+    } else if (dt == dt_recomb) {
+      // ---- recombination (engine.py:154-175) ----
+      const int e_idx = emin;
+      const int h_idx = A.en[e_idx];
+      __syncthreads();
+      if (tid == 0 && a.events && n_ev < sm.ev_cap) {
+        int32_t* evp = a.events + 4 * (sm.ev_offset + n_ev);
+        evp[0] = i;
+        evp[1] = 1;
+        evp[2] = e_idx;
+        evp[3] = h_idx;
+      }
+      ++n_ev;
+      // np.delete of electron row e_idx and hole h_idx: shift the tails down
+      const int ne_tail = n_e - 1 - e_idx, nh_tail = n_h - 1 - h_idx;
+      for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
+        const int k = base + tid;
+        double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
+        int n0 = 0;
+        if (k < ne_tail) {
+          const int s = e_idx + 1 + k;
+          x0 = A.ex[s];
+          y0 = A.ey[s];
+          z0 = A.ez[s];
+          d0 = A.ed[s];
+          n0 = A.en[s];
+        }
+        if (k < nh_tail) {
+          const int s = h_idx + 1 + k;
+          hx0 = A.hx[s];
+          hy0 = A.hy[s];
+          hz0 = A.hz[s];
+        }
+        __syncthreads();
+        if (k < ne_tail) {
+          const int dst = e_idx + k;
+          A.ex[dst] = x0;
+          A.ey[dst] = y0;
+          A.ez[dst] = z0;
+          A.ed[dst] = d0;
+          A.en[dst] = n0;
+        }
+        if (k < nh_tail) {
+          const int dst = h_idx + k;
+          A.hx[dst] = hx0;
+          A.hy[dst] = hy0;
+          A.hz[dst] = hz0;
+        }
+        __syncthreads();
+      }
+      --n_e;
+      --n_h;
+      if (tid == 0) sh.n_mask = 0;
+      __syncthreads();
+      for (int e = tid; e < n_e; e += BLOCK) {
+        int nn = A.en[e];
+        if (nn > h_idx) A.en[e] = --nn;
+        if (nn == h_idx) A.mlist[atomicAdd(&sh.n_mask, 1)] = e;
+      }
+      __syncthreads();
+      const int n_mask = sh.n_mask;
+      if (n_mask > 0 && n_h == 0) {
+        status = MCL_ENOHOLE;
+        break;
+      }
+      for (int m = 0; m < n_mask; ++m) {
+        const int e = A.mlist[m];
+        double dn;
+        int hn;
+        nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], dn, hn);
+        if (tid == 0) {
+          A.ed[e] = dn;
+          A.en[e] = hn;
+        }
+        __syncthreads();
+      }
+      ev = 1.0;
+    }
+    if (tid == 0) {
+      a.lum[out + i] = ev;
+      a.ratio[out + i] = __ddiv_rn((double)n_e, sm.N_e);
+    }
+    ++i;
+    if (sm.duration != 0.0 && t >= sm.duration) break;
+  }
+  if (tid == 0) {
+    a.n_steps[si] = i;
+    a.n_events[si] = n_ev;
+    a.draws[si] = S.pos;
+    a.status[si] = status;
+  }
+  __syncthreads();
+  return status;
+}
+
+template <int BLOCK, bool SMEM_ARRAYS>
+__global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap_max, int h_cap_max) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ Shared sh;
+  Source S;
+  S.rng = a.rng;
+  S.u = a.uniforms;
+  S.k0 = (uint32_t)a.seed;
+  S.k1 = (uint32_t)(a.seed >> 32);
+  S.mt = reinterpret_cast<uint32_t*>(smem);
+  S.ring = S.mt + 640;
+  unsigned char* arr_base = smem + sizeof(uint32_t) * (640 + kRing);
+  S.rd = S.wr = 0;
+  if (a.rng == MCL_RNG_MT19937) {
+    // load the key array and position; queue the untaken words of the current block
+    for (int k = threadIdx.x; k < kMtN; k += BLOCK) S.mt[k] = a.mt_state[k];
+    __syncthreads();
+    const uint32_t p = a.mt_state[kMtN];
+    for (int k = threadIdx.x + (int)p; k < kMtN; k += BLOCK) S.ring[k - p] = mt_temper(S.mt[k]);
+    S.wr = kMtN - p;
+    __syncthreads();
+  }
+  const int first = a.sequential ? 0 : blockIdx.x;
+  const int last = a.sequential ? a.n_sims : blockIdx.x + 1;
+  for (int si = first; si < last; ++si) {
+    const mcl_k_sim sm = a.sims[si];
+    S.stream = sm.stream_id;
+    if (!a.sequential || si == first) {
+      S.u_base = sm.u_offset;
+      S.u_count = sm.u_count;
+    }
+    unsigned char* base = SMEM_ARRAYS ? arr_base : reinterpret_cast<unsigned char*>(a.workspace) + sm.ws_offset;
+    const Arrays A = carve(base, SMEM_ARRAYS ? e_cap_max : sm.e_cap, SMEM_ARRAYS ? h_cap_max : sm.h_cap);
+    if (run_sim<BLOCK>(a, si, sm, A, sh, S) != MCL_OK && a.sequential) break;
+    // sequential runs share one injected stream: the next simulation starts
+    // where this one stopped (like the reference's global RandomState)
+    S.u_base += S.pos;
+    S.u_count -= S.pos;
+  }
+  if (a.rng == MCL_RNG_MT19937 && a.sequential) {
+    // the unread ring words all come from the last block: position = 624 - left
+    for (int k = threadIdx.x; k < kMtN; k += BLOCK) a.mt_state[k] = S.mt[k];
+    if (threadIdx.x == 0) a.mt_state[kMtN] = (uint32_t)(kMtN - (int)(S.wr - S.rd));
+  }
+}
+
+constexpr size_t kFixedSmem = sizeof(uint32_t) * (640 + kRing);
+constexpr size_t kMaxSmem = 220 * 1024;
+
+}  // namespace
+}  // namespace mcl
+
+using namespace mcl;
+
+extern "C" int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng, int32_t block,
+                              int64_t n_uniforms, int32_t* arrays_in_smem, int64_t* workspace_bytes,
+                              int32_t* e_cap_max, int32_t* h_cap_max) {
+  if (n_sims < 0 || (n_sims > 0 && !sims)) return MCL_EINVAL;
+  if (rng != MCL_RNG_PHILOX && rng != MCL_RNG_INJECTED && rng != MCL_RNG_MT19937) return MCL_EINVAL;
+  if (block != 256 && block != 512) return MCL_EINVAL;
+  int e_max = 0, h_max = 0;
+  int64_t ws = 0;
+  for (int32_t i = 0; i < n_sims; ++i) {
+    const mcl_k_sim& s = sims[i];
+    if (s.e0 < 0 || s.n_h0 < 0 || s.e_cap < s.e0 || s.h_cap < s.n_h0 || s.steps < 0) return MCL_EINVAL;
+    if (s.ev_cap < 0 || s.ev_offset < 0 || s.out_offset < 0 || s.ws_offset < 0) return MCL_EINVAL;
+    if (!(s.N_e > 0) || !std::isfinite(s.duration) || !std::isfinite(s.T_rate)) return MCL_EINVAL;
+    if (rng == MCL_RNG_INJECTED && (s.u_offset < 0 || s.u_count < 0 || s.u_offset + s.u_count > n_uniforms))
+      return MCL_ECAPACITY;
+    if (s.ws_offset % 16) return MCL_EINVAL;
+    e_max = s.e_cap > e_max ? s.e_cap : e_max;
+    h_max = s.h_cap > h_max ? s.h_cap : h_max;
+    const int64_t end = s.ws_offset + (int64_t)arrays_bytes(s.e_cap, s.h_cap);
+    ws = end > ws ? end : ws;
+  }
+  const bool fits = kFixedSmem + arrays_bytes(e_max, h_max) <= kMaxSmem;
+  if (arrays_in_smem) *arrays_in_smem = fits ? 1 : 0;
+  if (workspace_bytes) *workspace_bytes = fits ? 0 : ws;
+  if (e_cap_max) *e_cap_max = e_max;
+  if (h_cap_max) *h_cap_max = h_max;
+  return MCL_OK;
+}
+
+namespace {
+template <int BLOCK>
+int launch_k(const mcl_k_args& a, cudaStream_t s) {
+  const bool in_smem = a.arrays_in_smem != 0;
+  const size_t smem = kFixedSmem + (in_smem ? arrays_bytes(a.e_cap_max, a.h_cap_max) : 0);
+  if (smem > kMaxSmem) return MCL_ECAPACITY;
+  if (!in_smem && !a.workspace) return MCL_EINVAL;
+  auto fn = in_smem ? kk_kernel<BLOCK, true> : kk_kernel<BLOCK, false>;
+  MCL_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = a.sequential ? 1 : a.n_sims;
+  fn<<<grid, BLOCK, smem, s>>>(a, a.e_cap_max, a.h_cap_max);
+  MCL_CUDA_TRY(cudaGetLastError());
+  return MCL_OK;
+}
+}  // namespace
+
+extern "C" int mcl_k_run(const mcl_k_args* args, void* stream) {
+  if (!args) return MCL_EINVAL;
+  const mcl_k_args& a = *args;
+  if (a.n_sims == 0) return MCL_OK;
+  if (a.n_sims < 0 || !a.sims || !a.x_ax || !a.lum || !a.ratio || !a.n_events || !a.n_steps ||
+      !a.draws || !a.status)
+    return MCL_EINVAL;
+  if (a.rng == MCL_RNG_INJECTED && !a.uniforms) return MCL_EINVAL;
+  if (a.rng == MCL_RNG_MT19937 && (!a.mt_state || !a.sequential)) return MCL_EINVAL;
+  if (a.rng != MCL_RNG_PHILOX && a.rng != MCL_RNG_INJECTED && a.rng != MCL_RNG_MT19937) return MCL_EINVAL;
+  if (a.e_cap_max < 0 || a.h_cap_max < 0) return MCL_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (a.block == 256) return launch_k<256>(a, s);
+  if (a.block == 512) return launch_k<512>(a, s);
+  return MCL_EINVAL;
+}

@@ -1,0 +1,306 @@
+"""Drop-in for the reference's ``simulate(cfg)``: the event-driven kinetics on the GPU.
+
+``simulate(cfg)`` takes the same configuration (a dict or an OmegaConf
+``DictConfig`` with ``exp_type_fp`` / ``physics_fp`` groups), expands it with
+``initialize_runs`` (src/class/engine.py:13-38), reads each run's parameters the
+way src/class/simulate.py:39-45 and src/class/tl_trap_lab.py:27-43 do, runs every
+(run, sim) on the GPU (``mcl_k_run``) and returns ``(x_ax, Lum,
+electron_ratio, configs)`` shaped ``(steps, sims, runs)`` like
+src/class/simulate.py:30-32,112.
+
+Random numbers: by default the kernel draws from numpy's *global* legacy
+``RandomState`` (MT19937): its state is read before the call and advanced
+after it, exactly as the reference's ``np.random`` calls would advance it, so
+``np.random.seed(k); simulate(cfg)`` gives the reference's result for the same
+seed (up to the last bit of ``exp``/``log``, which can differ between numpy's
+and CUDA's implementations and, very rarely, flip a near-tie).  The
+simulations then run one after another on one CTA, as they share that stream.
+``rng="philox"`` gives each simulation its own counter-based stream and runs
+them all in parallel (one CTA each).
+
+Errors follow the reference: unknown or missing physics keys raise
+``TypeError`` (``Physics(**cfg.physics_fp)``, tl_trap_lab.py:30), more steps
+than table rows raise ``IndexError`` (simulate.py:64), a nearest search over no
+holes raises ``ValueError`` (numpy's empty ``min``).
+"""
+from __future__ import annotations
+
+import csv
+import ctypes as C
+from dataclasses import dataclass
+from typing import Any, Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .config import initialize_runs
+
+K_B_DEFAULT = 8.617333262145e-5  # src/class/engine.py:60
+PHYSICS_FIELDS = ("alpha", "b", "s", "E_cb", "E_loc_1", "E_loc_2", "D0", "Retrap",
+                  "name", "D", "rho_trap", "k_b")
+PHYSICS_REQUIRED = PHYSICS_FIELDS[:8]
+
+K_SIM_DTYPE = _lib.K_SIM_DTYPE
+KArgs = _lib.KArgs
+
+
+def _get(d: Any, k: str, default: Any = None) -> Any:
+    try:
+        return d.get(k, default)
+    except AttributeError:
+        return getattr(d, k, default)
+
+
+def physics(ph: Any) -> Dict[str, float]:
+    """The checks ``Physics(**cfg.physics_fp)`` performs (engine.py:44-60)."""
+    keys = list(ph.keys())
+    for k in keys:
+        if k not in PHYSICS_FIELDS:
+            raise TypeError(f"Physics.__init__() got an unexpected keyword argument '{k}'")
+    missing = [k for k in PHYSICS_REQUIRED if k not in keys]
+    if missing:
+        raise TypeError(f"Physics.__init__() missing {len(missing)} required positional "
+                        f"argument{'s' if len(missing) > 1 else ''}: "
+                        + ", ".join(f"'{m}'" for m in missing))
+    out = {k: float(ph[k]) for k in PHYSICS_REQUIRED}
+    out["k_b"] = float(_get(ph, "k_b", K_B_DEFAULT))
+    return out
+
+
+@dataclass
+class RunParams:
+    """One run's parameters, read as simulate.py:39-48 and tl_trap_lab.py:27-43 read them."""
+    phys: Dict[str, float]
+    duration: float
+    e_ratio_start: float
+    dose_rate: float
+    T_rate: float
+    dt_cap: float
+    T_start: float
+    N_e: float
+    L: float
+    Lb: float
+    e0: int
+    n_h0: int
+
+
+def run_params(run_cfg: Any, dose_rate: Optional[float] = None) -> RunParams:
+    mc = run_cfg["exp_type_fp"]
+    ph = run_cfg["physics_fp"]
+    duration = float(_get(mc, "duration", 0.0))
+    e_ratio_start = float(_get(mc, "e_ratio_start", 0.0))
+    # simulate.py:42 reads the key "dose_rate" (the YAML files call it "D");
+    # Physics(**physics_fp) would reject that key, so only the keyword
+    # argument of this function can switch filling on.
+    dr = float(_get(ph, "dose_rate", 0.0)) if dose_rate is None else float(dose_rate)
+    T_rate = float(_get(mc, "T_rate", 0.0))
+    max_dt = float(_get(mc, "max_dt", 0.5))
+    dt_cap = max_dt / T_rate if T_rate else 1e20
+    p = physics(ph)
+    T_start = _get(mc, "T_start", 0)
+    rho = mc["rho_prime"] * (3 / (4 * np.pi) * p["alpha"] ** 3)
+    d = (mc["holes"] / rho) ** (1 / 3)
+    bf = mc["boundary_factor"]
+    e0 = int(mc["N_e"] * e_ratio_start)
+    n_h0 = int(mc["holes"] * bf ** 3)
+    return RunParams(p, duration, e_ratio_start, dr, T_rate, dt_cap, float(T_start),
+                     float(mc["N_e"]), float(d), float(d * bf), e0, n_h0)
+
+
+@dataclass
+class KResult:
+    x_ax: np.ndarray              # (steps, n_sims)
+    lum: np.ndarray
+    electron_ratio: np.ndarray
+    n_steps: np.ndarray           # (n_sims,)
+    draws: np.ndarray
+    status: np.ndarray
+    events: List[np.ndarray]      # per simulation (n, 4): step, kind, e_idx, h_idx
+
+
+def _fill_sims(params: Sequence[RunParams], steps: int, extra: int):
+    sims = np.zeros(len(params), dtype=K_SIM_DTYPE)
+    for i, rp in enumerate(params):
+        r = sims[i]
+        for k, v in rp.phys.items():
+            r[k] = v
+        r["dose_rate"], r["T_start"], r["T_rate"] = rp.dose_rate, rp.T_start, rp.T_rate
+        r["dt_cap"], r["duration"], r["N_e"] = rp.dt_cap, rp.duration, rp.N_e
+        r["L"] = r["W"] = r["H"] = rp.L
+        r["Lb"] = r["Wb"] = r["Hb"] = rp.Lb
+        r["e0"], r["n_h0"] = rp.e0, rp.n_h0
+        e_cap = max(rp.e0, int(rp.N_e)) + extra
+        r["e_cap"] = e_cap
+        r["h_cap"] = rp.n_h0 + (e_cap - rp.e0)
+        r["steps"] = steps
+        r["stream_id"] = i
+        r["out_offset"] = i * steps
+        r["ev_offset"] = i * steps
+        r["ev_cap"] = steps
+    return sims
+
+
+def _ws_offsets(sims: np.ndarray) -> int:
+    """Place each simulation's arrays in the workspace (global-memory mode)."""
+    off = 0
+    for r in sims:
+        r["ws_offset"] = off
+        e, h = int(r["e_cap"]), int(r["h_cap"])
+        a16 = lambda x: (x + 15) & ~15
+        off += a16(32 * e) + a16(4 * e) + a16(e) + a16(4 * e) + a16(24 * h)
+    return off
+
+
+def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox", seed: int = 0,
+                 mt_state=None, uniforms: Optional[np.ndarray] = None, sequential: Optional[bool] = None,
+                 block: int = 256, extra_capacity: int = 64, want_events: bool = True):
+    """Run simulations on the GPU.  ``rng``: "philox" (independent streams,
+    parallel), "mt19937" (one shared stream continuing from ``mt_state``, a
+    numpy legacy state tuple, sequential) or "injected" (``uniforms``; shared
+    and sequential unless ``sequential=False``, then each simulation starts
+    at ``u_offset``).  Returns (KResult, final mt_state or None)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required (the library has no CPU path)")
+    lib = _lib.load()
+    code = {"philox": _lib.MCL_RNG_PHILOX, "injected": _lib.MCL_RNG_INJECTED,
+            "mt19937": _lib.MCL_RNG_MT19937}[rng]
+    if sequential is None:
+        sequential = rng != "philox"
+    n = len(params)
+    sims = _fill_sims(params, steps, extra_capacity)
+    n_u = 0
+    if rng == "injected":
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        n_u = int(u.size)
+        if sequential:
+            sims["u_offset"][0] = 0
+            sims["u_count"][0] = n_u
+    smem_flag, ws_need = C.c_int32(), C.c_int64()
+    e_max, h_max = C.c_int32(), C.c_int32()
+    ws_bytes = _ws_offsets(sims)
+    _lib.check(lib.mcl_k_validate(_lib.ptr(sims), n, code, block, n_u, C.byref(smem_flag),
+                                  C.byref(ws_need), C.byref(e_max), C.byref(h_max)), "mcl_k_validate")
+    dev = torch.device("cuda")
+    d_sims = torch.from_numpy(sims.view(np.uint8)).to(dev)
+    rows = max(n * steps, 1)
+    x_ax = torch.zeros(rows, dtype=torch.float64, device=dev)
+    lum = torch.zeros_like(x_ax)
+    ratio = torch.zeros_like(x_ax)
+    events = torch.zeros(max(4 * n * steps, 4), dtype=torch.int32, device=dev) if want_events else None
+    n_ev = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    n_st = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    draws = torch.zeros(max(n, 1), dtype=torch.int64, device=dev)
+    status = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    d_u = torch.from_numpy(u).to(dev) if rng == "injected" else None
+    d_mt = None
+    if rng == "mt19937":
+        name, keys, pos = mt_state[0], mt_state[1], mt_state[2]
+        if name != "MT19937":
+            raise ValueError("expected a legacy MT19937 state")
+        st = np.zeros(625, dtype=np.uint32)
+        st[:624] = np.asarray(keys, dtype=np.uint32)
+        st[624] = int(pos)
+        d_mt = torch.from_numpy(st.view(np.int32)).to(dev)
+    d_ws = (torch.zeros(max(ws_bytes, 16), dtype=torch.uint8, device=dev)
+            if not smem_flag.value else None)
+    a = KArgs()
+    a.sims, a.x_ax, a.lum, a.ratio = _lib.ptr(d_sims), _lib.ptr(x_ax), _lib.ptr(lum), _lib.ptr(ratio)
+    a.events, a.n_events, a.n_steps = _lib.ptr(events), _lib.ptr(n_ev), _lib.ptr(n_st)
+    a.draws, a.status, a.uniforms = _lib.ptr(draws), _lib.ptr(status), _lib.ptr(d_u)
+    a.mt_state, a.workspace = _lib.ptr(d_mt), _lib.ptr(d_ws)
+    a.workspace_bytes = int(d_ws.numel()) if d_ws is not None else 0
+    a.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    a.n_sims, a.rng, a.sequential, a.block = n, code, int(bool(sequential)), block
+    a.e_cap_max, a.h_cap_max, a.arrays_in_smem = e_max.value, h_max.value, smem_flag.value
+    s = torch.cuda.current_stream()
+    _lib.check(lib.mcl_k_run(C.byref(a), C.c_void_p(s.cuda_stream)), "mcl_k_run")
+    s.synchronize()
+    st_h = status.cpu().numpy()[:n]
+    nst = n_st.cpu().numpy()[:n]
+    nev = n_ev.cpu().numpy()[:n]
+    ev_h = events.cpu().numpy().reshape(-1, 4) if want_events else None
+    evs = []
+    for i in range(n):
+        if want_events:
+            k = min(int(nev[i]), steps)
+            evs.append(ev_h[i * steps:i * steps + k].astype(np.int64))
+        else:
+            evs.append(None)
+    res = KResult(x_ax.cpu().numpy().reshape(n, steps).T.copy(), lum.cpu().numpy().reshape(n, steps).T.copy(),
+                  ratio.cpu().numpy().reshape(n, steps).T.copy(), nst, draws.cpu().numpy()[:n], st_h, evs)
+    new_state = None
+    if d_mt is not None:
+        st = d_mt.cpu().numpy().view(np.uint32)
+        new_state = ("MT19937", st[:624].copy(), int(st[624]))
+    return res, new_state
+
+
+def _raise_for(status: np.ndarray, steps: int):
+    for code in status:
+        code = int(code)
+        if code == _lib.MCL_EOVERFLOW:
+            raise IndexError(f"index {steps} is out of bounds for axis 0 with size {steps}")
+        if code == _lib.MCL_ENOHOLE:
+            raise ValueError("zero-size array to reduction operation minimum which has no identity")
+        if code != _lib.MCL_OK:
+            raise _lib.MclError(code, "event-driven kinetics kernel")
+
+
+def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,
+             dose_rate: Optional[float] = None, csv_path: Optional[str] = None,
+             block: int = 256, return_result: bool = False):
+    """GPU replacement of src/class/simulate.py:simulate.
+
+    ``rng="numpy"`` continues numpy's global legacy RandomState (seeded with
+    ``seed`` first when given); ``rng="philox"`` uses independent Philox
+    streams keyed by ``seed``.  ``dose_rate`` switches trap filling on (the
+    reference reads it from ``physics_fp.dose_rate``, a key its Physics class
+    rejects).  ``csv_path`` writes the long table of simulate.py:95-110.
+    """
+    configs = initialize_runs(cfg)
+    n_runs = len(configs)
+    mc0 = configs[0]["exp_type_fp"]
+    steps = int(mc0["steps"])
+    sims = int(mc0["sims"])
+    params = []
+    for ri in range(n_runs):
+        rp = run_params(configs[ri], dose_rate)
+        params += [rp] * sims
+    extra = 64
+    while True:
+        if rng == "numpy":
+            if seed is not None:
+                np.random.seed(seed)
+            state0 = np.random.get_state()
+            res, new_state = run_kinetics(params, steps, rng="mt19937", mt_state=state0, block=block,
+                                          extra_capacity=extra)
+        else:
+            res, new_state = run_kinetics(params, steps, rng="philox", seed=seed or 0, block=block,
+                                          extra_capacity=extra)
+        if np.any(res.status == _lib.MCL_ECAPACITY) and extra < 1 << 20:
+            extra *= 8    # more pair creations than provisioned: run again with room
+            continue
+        break
+    if rng == "numpy":
+        np.random.set_state(("MT19937", new_state[1], new_state[2], state0[3], state0[4]))
+    _raise_for(res.status, steps)
+    x_ax = res.x_ax.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
+    lum = res.lum.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
+    ratio = res.electron_ratio.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
+    if csv_path:
+        write_table(csv_path, lum, ratio)
+    out = (x_ax, lum, ratio, configs)
+    return (out, res) if return_result else out
+
+
+def write_table(path: str, lum: np.ndarray, ratio: np.ndarray) -> None:
+    """Long table run,sim,step,lum,electron_ratio (src/class/simulate.py:95-110)."""
+    steps, sims, runs = lum.shape
+    with open(path, "w", newline="") as f:
+        w = csv.writer(f)
+        w.writerow(["run", "sim", "step", "lum", "electron_ratio"])
+        for r in range(runs):
+            for s in range(sims):
+                for k in range(steps):
+                    w.writerow([r, s, k, repr(float(lum[k, s, r])), repr(float(ratio[k, s, r]))])

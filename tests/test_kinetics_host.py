@@ -1,0 +1,35 @@
+"""Host-side logic of the event-driven drop-in (no GPU needed)."""
+import numpy as np
+import pytest
+
+from golden_io import k_case, load_k
+from mcluminescence_gb300.config import initialize_runs
+from mcluminescence_gb300.kinetics import physics, run_params
+from oracle import kinetics_k as ok
+
+DATA = load_k()
+
+
+@pytest.mark.parametrize("name", ["tl12_full", "lab_physics", "cold_isothermal", "config1_shape"])
+def test_run_params_geometry_matches_oracle(name):
+    cfg = k_case(DATA, name)["cfg"]
+    for r in initialize_runs(cfg).values():
+        rp = run_params(r)
+        kr = ok.run_from_cfg(r)
+        d, e0, nh, core, bound = ok.box_geometry(kr)
+        assert rp.L == d and rp.Lb == bound[0] and rp.e0 == e0 and rp.n_h0 == nh
+        assert rp.dt_cap == (kr.max_dt / kr.T_rate if kr.T_rate else 1e20)
+
+
+def test_physics_keys_behave_like_the_dataclass():
+    good = {"alpha": 1.0, "b": 1.0, "s": 1.0, "E_cb": 1.0, "E_loc_1": 1.0, "E_loc_2": 1.0,
+            "D0": 1.0, "Retrap": 0.5, "name": "x", "D": 0, "k_b": 8.6e-5}
+    assert physics(good)["k_b"] == 8.6e-5
+    with pytest.raises(TypeError, match="unexpected keyword argument 'E'"):
+        physics(dict(good, E=1.2))                # conf/physics_fp/BG_basic.yaml
+    with pytest.raises(TypeError, match="unexpected keyword argument 'dose_rate'"):
+        physics(dict(good, dose_rate=0.1))
+    bad = dict(good)
+    del bad["Retrap"]
+    with pytest.raises(TypeError, match="missing 1 required"):
+        physics(bad)

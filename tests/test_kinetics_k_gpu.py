@@ -1,0 +1,87 @@
+"""The event-driven (reference) kinetics kernel against the reference's own
+outputs (golden fixtures made by running the unmodified reference)."""
+import numpy as np
+import pytest
+
+from golden_io import k_case, k_case_names, load_k
+from mcluminescence_gb300 import run_kinetics, run_params, simulate
+from mcluminescence_gb300.config import initialize_runs
+
+pytestmark = pytest.mark.gpu
+
+DATA = load_k()
+CASES = [c for c in k_case_names(DATA) if c != "box_ops"]
+
+
+def _check_against_golden(case, x_ax, lum, ratio, res):
+    # integer outcomes exactly; times to the last bits of exp/log
+    assert np.array_equal(lum, case["lum"])
+    assert np.array_equal(ratio, case["electron_ratio"])
+    np.testing.assert_allclose(x_ax, case["x_ax"], rtol=1e-12, atol=0)
+    assert list(res.n_steps) == list(case["steps_taken"])
+    assert list(res.draws) == list(case["draws"])
+    for got, want in zip(res.events, case["events"]):
+        assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_simulate_matches_reference_draw_for_draw(name):
+    """np.random.seed(k); simulate(cfg) on the GPU == the reference's simulate(cfg)."""
+    case = k_case(DATA, name)
+    np.random.seed(case["seed"])
+    if case["error"]:
+        with pytest.raises(IndexError):
+            simulate(case["cfg"])
+        return
+    (x_ax, lum, ratio, configs), res = simulate(case["cfg"], return_result=True)
+    _check_against_golden(case, x_ax, lum, ratio, res)
+    # numpy's global stream is left where the reference leaves it
+    after = np.random.random_sample(3)
+    rs = np.random.RandomState(case["seed"])
+    rs.random_sample(int(np.sum(case["draws"])))
+    assert np.array_equal(after, rs.random_sample(3))
+
+
+@pytest.mark.parametrize("name", ["tl12_small", "lab_physics", "cold_isothermal", "isothermal"])
+def test_injected_stream_equals_mt_stream(name):
+    """The same draws handed over as an injected array give the same results."""
+    case = k_case(DATA, name)
+    cfg = case["cfg"]
+    sims = int(cfg["exp_type_fp"]["sims"])
+    params = []
+    for r in initialize_runs(cfg).values():
+        params += [run_params(r)] * sims
+    u = np.random.RandomState(case["seed"]).random_sample(int(np.sum(case["draws"])))
+    steps = int(cfg["exp_type_fp"]["steps"])
+    res, _ = run_kinetics(params, steps, rng="injected", uniforms=u)
+    assert list(res.status) == [0] * len(params)
+    assert list(res.draws) == list(case["draws"])
+    for got, want in zip(res.events, case["events"]):
+        assert np.array_equal(got, want)
+
+
+def test_injected_stream_too_short_is_reported():
+    case = k_case(DATA, "tl12_small")
+    cfg = case["cfg"]
+    params = [run_params(initialize_runs(cfg)[0])]
+    u = np.random.RandomState(0).random_sample(1000)
+    res, _ = run_kinetics(params, int(cfg["exp_type_fp"]["steps"]), rng="injected", uniforms=u)
+    from mcluminescence_gb300 import _lib
+    assert res.status[0] == _lib.MCL_EBUDGET
+
+
+def test_philox_parallel_statistics_and_determinism():
+    """Independent Philox streams, all simulations in parallel: same event
+    totals as the reference's runs within Monte Carlo scatter, and the same
+    results when repeated."""
+    case = k_case(DATA, "tl12_small")
+    cfg = dict(case["cfg"])
+    cfg["exp_type_fp"] = dict(cfg["exp_type_fp"], sims=64)
+    (x1, l1, r1, _), = [simulate(cfg, rng="philox", seed=3)]
+    x2, l2, r2, _ = simulate(cfg, rng="philox", seed=3)
+    assert np.array_equal(l1, l2) and np.array_equal(x1, x2)
+    ref = case["lum"].sum(axis=0)          # (sims=2, runs=3) reference totals
+    got = l1.sum(axis=0)                   # (64, 3)
+    for r in range(3):
+        m, s = got[:, r].mean(), got[:, r].std(ddof=1)
+        assert abs(ref[:, r].mean() - m) < 4 * s + 1

@@ -35,9 +35,10 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_struct_layout(lib):
-    sizes = (C.c_size_t * 4)()
+    sizes = (C.c_size_t * 6)()
     assert lib.mcl_struct_sizes(sizes) == 0
-    assert tuple(sizes) == (64, 96, 8, C.sizeof(_lib.BArgs))
+    assert tuple(sizes) == (64, 96, 8, C.sizeof(_lib.BArgs), _lib.K_SIM_DTYPE.itemsize,
+                            C.sizeof(_lib.KArgs))
 
 
 def test_device_info_without_gpu(lib):
