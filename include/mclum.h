@@ -256,6 +256,36 @@ int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng, int32_t b
  * injected stream runs out, MCL_ENOHOLE for a nearest search over no holes. */
 int mcl_k_run(const mcl_k_args* args, void* stream);
 
+/* ---- surrogate network (no counterpart in the reference) ------------------ */
+/* The reference fits parameters by running the Monte Carlo for every
+ * candidate (src/class/optimizer.py:93-111); these kernels train and run a
+ * small MLP (6 -> 256 -> 256 -> 256 -> 256 -> 200, GELU) that proposes
+ * candidates instead.  bf16 tensors are passed as void* (2-byte elements).  */
+#define MCL_EPI_F32 0        /* C = A B^T                                      */
+#define MCL_EPI_BIAS 1       /* C = A B^T + bias                               */
+#define MCL_EPI_BIAS_GELU 2  /* C = A B^T + bias; Y = gelu(C) (bf16), Yt = Y^T */
+/* C[M][N] (fp32) = sum_k A[m][k] B[n][k] with BF16 operands (k contiguous),
+ * FP32 accumulation on the tensor cores and a fused epilogue.  M, N multiples
+ * of 64, K of 32; leading dimensions in elements, multiples of 8. */
+int mcl_gemm_nt(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
+                const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
+                int32_t ldy, void* Yt, int32_t ldyt, void* stream);
+/* dZ = dY * gelu'(Z) (or dY when gelu_on == 0) as bf16 in [M][N] and [N][M];
+ * db[n] += sum_m dZ[m][n] (db must be cleared by the caller). */
+int mcl_act_backward(int32_t M, int32_t N, const float* dY, int32_t lddy, const float* Z, int32_t ldz,
+                     int32_t gelu_on, void* dZ, int32_t lddz, void* dZt, int32_t lddzt, float* db,
+                     void* stream);
+/* *loss += sum over columns < n_valid of (out - target)^2;
+ * dout = 2 (out - target) * scale (0 in the padding columns). */
+int mcl_mse_loss(int32_t M, int32_t N, int32_t n_valid, const float* out, int32_t ldo,
+                 const float* target, int32_t ldt, float scale, float* dout, int32_t ldd, float* loss,
+                 void* stream);
+/* Adam step on fp32 master weights p[rows][cols]; refreshes the bf16 copies
+ * W[rows][cols] and Wt[cols][rows] when non-null.  step counts from 1. */
+int mcl_adam(int32_t rows, int32_t cols, float* p, const float* g, float* m1, float* m2, float lr,
+             float b1, float b2, float eps, int32_t step, void* W, void* Wt, void* stream);
+int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream);
+
 /* ---- CUDA graphs -------------------------------------------------------- */
 /* Capture mcl_b_run(args) (with its output clearing) into a graph. */
 int mcl_b_graph_create(const mcl_b_args* args, void* stream, void** graph_out);

@@ -1,0 +1,308 @@
+"""Learned surrogate of the Monte Carlo glow curve, trained on the GPU.
+
+A small MLP maps six physics parameters -- trap depth E, log10 s, the
+tunnelling coefficient alpha, log10 rho', log10 dose and log10 heating rate --
+to the 200-bin log glow curve that the Monte Carlo kernel produces (TL ramp
+0 -> 500 degC, 2.5 degC bins, 2,000 traps).  Forward, backward and Adam run in
+the library's own kernels (``mcl_gemm_nt`` with fused bias+GELU epilogue on
+BF16 operands with FP32 accumulation, ``mcl_act_backward``, ``mcl_mse_loss``,
+``mcl_adam``); torch only provides device memory and the stream.
+
+The reference has no surrogate: its optimiser (src/class/optimizer.py:93-111)
+evaluates every differential-evolution candidate with a full simulation.  Here
+the surrogate proposes candidates and the Monte Carlo verifies them.
+
+Physics of the training curves (the batched kernel's Bernoulli mode):
+effective tunnelling coefficient alpha_eff = alpha * (1e-6 / rho')^(1/3)
+(the centre spacing scales as rho'^(-1/3)), initial fill
+N (1 - exp(-dose / D0)) with D0 = 200 Gy, TL ramp from 0 degC at beta K/s.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .schedule import SetSpec, Segment, C_TO_K
+
+DIMS = (6, 256, 256, 256, 256, 200)
+IN_PAD = 64
+OUT_PAD = 256
+N_TRAPS = 2000
+D0_GY = 200.0
+N_BINS = 200
+BIN_C = 2.5
+EPS_Y = 1e-4
+
+# parameter ranges: E, log10 s, alpha, log10 rho', log10 dose, log10 beta
+LOW = np.array([1.2, 10.0, 2.0, -7.0, 0.0, math.log10(0.5)])
+HIGH = np.array([1.8, 14.0, 12.0, -5.0, 3.0, math.log10(5.0)])
+
+
+def sample_params(n: int, rng: np.random.Generator) -> np.ndarray:
+    return LOW + (HIGH - LOW) * rng.random((n, 6))
+
+
+def standardize(p: np.ndarray) -> np.ndarray:
+    """Map each parameter's range to [-1, 1]."""
+    return 2.0 * (p - LOW) / (HIGH - LOW) - 1.0
+
+
+def curve_spec(p: Sequence[float], set_id: int, n_traps: int = N_TRAPS) -> SetSpec:
+    """The Monte Carlo set whose glow curve the surrogate learns for parameters p."""
+    E, log_s, alpha, log_rho, log_dose, log_beta = (float(x) for x in p)
+    beta = 10.0 ** log_beta
+    k = max(1, int(math.ceil(BIN_C / (beta * 0.1) - 1e-9)))   # steps per 2.5 degC bin, dt <= 0.1 s
+    dt = BIN_C / (beta * k)
+    a_eff = alpha * (1e-6 / 10.0 ** log_rho) ** (1.0 / 3.0)
+    filled = int(round(n_traps * (1.0 - math.exp(-(10.0 ** log_dose) / D0_GY))))
+    seg = Segment(n_steps=N_BINS * k, dt=dt, steps_per_bin=k, T0=C_TO_K, beta=beta)
+    return SetSpec(n_slots=n_traps, n_filled=filled, E=E, s=10.0 ** log_s, alpha=a_eff,
+                   segments=[seg], set_id=set_id, kind="tl_curve").finalize()
+
+
+def simulate_curves(params: np.ndarray, seed: int, id0: int = 0, n_traps: int = N_TRAPS,
+                    chunk: int = 65536, precision: str = "fp32") -> np.ndarray:
+    """Monte Carlo glow curves (counts per bin, float32 [n][200]) on the GPU."""
+    from .batch import BernoulliBatch
+    import torch
+    out = np.zeros((len(params), N_BINS), dtype=np.float32)
+    for c0 in range(0, len(params), chunk):
+        sub = params[c0:c0 + chunk]
+        specs = [curve_spec(p, id0 + c0 + i, n_traps) for i, p in enumerate(sub)]
+        b = BernoulliBatch(specs, precision=precision, seed=seed, want_alive=False,
+                           block=128 if precision == "fp32" else 256, ept=8 if precision == "fp32" else 2)
+        b.launch()
+        torch.cuda.synchronize()
+        out[c0:c0 + len(sub)] = b.result().lum.reshape(len(sub), N_BINS)
+    return out
+
+
+def curve_to_target(counts: np.ndarray, n_traps: int = N_TRAPS) -> np.ndarray:
+    return np.log10(counts / n_traps + EPS_Y).astype(np.float32)
+
+
+def target_to_curve(y: np.ndarray, n_traps: int = N_TRAPS) -> np.ndarray:
+    return np.clip(10.0 ** y - EPS_Y, 0.0, None) * n_traps
+
+
+@dataclass
+class Layer:
+    W: object      # fp32 master [out][in]
+    b: object      # fp32 [out]
+    Wb: object     # bf16 [out][in]
+    Wt: object     # bf16 [in][out]
+    mW: object
+    vW: object
+    mb: object
+    vb: object
+    gW: object
+    gb: object
+
+
+class SurrogateMLP:
+    """The network with its device buffers for a fixed batch size."""
+
+    def __init__(self, batch: int = 4096, seed: int = 0, device: str = "cuda"):
+        import torch
+        assert batch % 64 == 0
+        self.torch = torch
+        self.lib = _lib.load()
+        self.B = batch
+        self.dev = torch.device(device)
+        g = torch.Generator().manual_seed(seed)
+        self.ins = [IN_PAD] + [256] * 4
+        self.outs = [256] * 4 + [OUT_PAD]
+        self.layers: List[Layer] = []
+        for l, (k, n) in enumerate(zip(self.ins, self.outs)):
+            fan_in = DIMS[l]
+            W = torch.zeros(n, k, dtype=torch.float32)
+            W[:DIMS[l + 1], :fan_in] = (torch.rand(DIMS[l + 1], fan_in, generator=g) * 2 - 1) / math.sqrt(fan_in)
+            b = torch.zeros(n, dtype=torch.float32)
+            W, b = W.to(self.dev), b.to(self.dev)
+            z = lambda *s: torch.zeros(*s, dtype=torch.float32, device=self.dev)
+            L = Layer(W, b, W.to(torch.bfloat16).contiguous(), W.t().contiguous().to(torch.bfloat16),
+                      z(n, k), z(n, k), z(n), z(n), z(n, k), z(n))
+            self.layers.append(L)
+        B = batch
+        bf = lambda *s: torch.zeros(*s, dtype=torch.bfloat16, device=self.dev)
+        f32 = lambda *s: torch.zeros(*s, dtype=torch.float32, device=self.dev)
+        self.x0 = bf(B, IN_PAD)
+        self.x0t = bf(IN_PAD, B)
+        self.Z = [f32(B, n) for n in self.outs]
+        self.Y = [bf(B, n) for n in self.outs[:-1]]
+        self.Yt = [bf(n, B) for n in self.outs[:-1]]
+        self.target = f32(B, OUT_PAD)
+        self.dOut = f32(B, OUT_PAD)
+        self.dY = [f32(B, k) for k in self.ins]
+        self.dZ = [bf(B, n) for n in self.outs]
+        self.dZt = [bf(n, B) for n in self.outs]
+        self.loss = f32(1)
+        self.step_count = 0
+
+    # -- plumbing -------------------------------------------------------------
+    def _s(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    @staticmethod
+    def _p(t):
+        return C.c_void_p(t.data_ptr()) if t is not None else None
+
+    def _gemm(self, epi, M, N, K, A, lda, Bm, ldb, bias, Cm, ldc, Y=None, ldy=0, Yt=None, ldyt=0):
+        _lib.check(self.lib.mcl_gemm_nt(epi, M, N, K, self._p(A), lda, self._p(Bm), ldb, self._p(bias),
+                                        self._p(Cm), ldc, self._p(Y), ldy, self._p(Yt), ldyt, self._s()),
+                   "mcl_gemm_nt")
+
+    # -- data -----------------------------------------------------------------
+    def set_inputs(self, x_std: "torch.Tensor") -> None:
+        """x_std: float tensor [B][6] of standardized parameters (device)."""
+        t = self.torch
+        x = t.zeros(self.B, IN_PAD, dtype=t.bfloat16, device=self.dev)
+        x[:, :6] = x_std.to(t.bfloat16)
+        self.x0.copy_(x)
+        self.x0t.copy_(x.t())
+
+    def set_targets(self, y: "torch.Tensor") -> None:
+        self.target[:, :DIMS[-1]].copy_(y)
+
+    # -- passes ---------------------------------------------------------------
+    def forward(self) -> "torch.Tensor":
+        B = self.B
+        A, lda = self.x0, IN_PAD
+        for l, L in enumerate(self.layers):
+            n, k = self.outs[l], self.ins[l]
+            if l < len(self.layers) - 1:
+                self._gemm(_lib_EPI.BIAS_GELU, B, n, k, A, lda, L.Wb, k, L.b, self.Z[l], n,
+                           self.Y[l], n, self.Yt[l], B)
+                A, lda = self.Y[l], n
+            else:
+                self._gemm(_lib_EPI.BIAS, B, n, k, A, lda, L.Wb, k, L.b, self.Z[l], n)
+        return self.Z[-1][:, :DIMS[-1]]
+
+    def backward(self, want_input_grad: bool = False) -> None:
+        """Gradients of the mean squared error (over batch and 200 bins)."""
+        t, B = self.torch, self.B
+        self.loss.zero_()
+        _lib.check(self.lib.mcl_mse_loss(B, OUT_PAD, DIMS[-1], self._p(self.Z[-1]), OUT_PAD,
+                                         self._p(self.target), OUT_PAD, C.c_float(1.0 / (B * DIMS[-1])),
+                                         self._p(self.dOut), OUT_PAD, self._p(self.loss), self._s()),
+                   "mcl_mse_loss")
+        dY, lddy = self.dOut, OUT_PAD
+        for l in range(len(self.layers) - 1, -1, -1):
+            L = self.layers[l]
+            n, k = self.outs[l], self.ins[l]
+            L.gb.zero_()
+            last = l == len(self.layers) - 1
+            _lib.check(self.lib.mcl_act_backward(B, n, self._p(dY), lddy, self._p(self.Z[l]), n,
+                                                 0 if last else 1, self._p(self.dZ[l]), n,
+                                                 self._p(self.dZt[l]), B, self._p(L.gb), self._s()),
+                       "mcl_act_backward")
+            Xt = self.Yt[l - 1] if l > 0 else self.x0t
+            # dW[n][k] = sum_m dZ[m][n] X[m][k]
+            self._gemm(_lib_EPI.F32, n, k, B, self.dZt[l], B, Xt, B, None, L.gW, k)
+            if l > 0 or want_input_grad:
+                # dX[m][k] = sum_n dZ[m][n] W[n][k]
+                self._gemm(_lib_EPI.F32, B, k, n, self.dZ[l], n, L.Wt, n, None, self.dY[l], k)
+            dY, lddy = self.dY[l], k
+
+    def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        self.step_count += 1
+        for L in self.layers:
+            n, k = L.W.shape
+            _lib.check(self.lib.mcl_adam(n, k, self._p(L.W), self._p(L.gW), self._p(L.mW), self._p(L.vW),
+                                         C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
+                                         self.step_count, self._p(L.Wb), self._p(L.Wt), self._s()),
+                       "mcl_adam")
+            _lib.check(self.lib.mcl_adam(1, n, self._p(L.b), self._p(L.gb), self._p(L.mb), self._p(L.vb),
+                                         C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
+                                         self.step_count, None, None, self._s()), "mcl_adam")
+
+    def input_grad(self) -> "torch.Tensor":
+        """d loss / d standardized input (after backward(want_input_grad=True))."""
+        return self.dY[0][:, :6]
+
+
+class _lib_EPI:
+    F32 = 0
+    BIAS = 1
+    BIAS_GELU = 2
+
+
+def reference_forward_backward(model: SurrogateMLP, x_std: np.ndarray, y: np.ndarray):
+    """The same network in float64 on the CPU (torch autograd) with the
+    model's bf16-rounded weights, inputs and hidden activations: loss and
+    parameter gradients.  Used by the gradient checks."""
+    import torch
+    t = torch
+    xb = t.tensor(x_std, dtype=t.float32).to(t.bfloat16).to(t.float64)
+    h = t.zeros(xb.shape[0], IN_PAD, dtype=t.float64)
+    h[:, :6] = xb
+    Ws, bs = [], []
+    for L in model.layers:
+        W = L.Wb.float().cpu().to(t.float64).requires_grad_(True)
+        b = L.b.cpu().to(t.float64).requires_grad_(True)
+        Ws.append(W)
+        bs.append(b)
+    for l in range(len(Ws)):
+        z = h @ Ws[l].t() + bs[l]
+        # hidden activations travel between layers in bf16, as on the GPU
+        h = t.nn.functional.gelu(z).to(t.bfloat16).to(t.float64) if l < len(Ws) - 1 else z
+    out = h[:, :DIMS[-1]]
+    yt = t.tensor(y, dtype=t.float64)
+    loss = ((out - yt) ** 2).mean()
+    loss.backward()
+    return float(loss.detach()), [W.grad.numpy() for W in Ws], [b.grad.numpy() for b in bs], out.detach().numpy()
+
+
+# ---------------------------------------------------------------------------
+# training and inference
+# ---------------------------------------------------------------------------
+def generate_dataset(n: int, seed: int, id0: int = 0, n_traps: int = N_TRAPS):
+    """n parameter draws and their Monte Carlo curves (counts), on the GPU."""
+    rng = np.random.default_rng(seed)
+    params = sample_params(n, rng)
+    counts = simulate_curves(params, seed=seed, id0=id0, n_traps=n_traps)
+    return params, counts
+
+
+def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: int = 4000,
+          lr: float = 2e-3, lr_final: float = 5e-5, seed: int = 0, log_every: int = 0,
+          n_traps: int = N_TRAPS) -> List[float]:
+    """Adam on random mini-batches; cosine decay from lr to lr_final.
+    Returns the loss (mean squared error of the log curve) every log_every steps."""
+    t = model.torch
+    X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
+    Y = t.tensor(curve_to_target(counts, n_traps), dtype=t.float32, device=model.dev)
+    gen = t.Generator(device=model.dev).manual_seed(seed)
+    hist = []
+    for k in range(steps):
+        idx = t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev)
+        model.set_inputs(X.index_select(0, idx))
+        model.set_targets(Y.index_select(0, idx))
+        model.forward()
+        model.backward()
+        cur = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps - 1, 1)))
+        model.adam_step(lr=cur)
+        if log_every and (k % log_every == 0 or k == steps - 1):
+            hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
+    return hist
+
+
+def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
+    """Predicted log curves [n][200] (float32, host)."""
+    t = model.torch
+    X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
+    n = X.shape[0]
+    out = np.zeros((n, DIMS[-1]), dtype=np.float32)
+    for c0 in range(0, n, model.B):
+        xb = X[c0:c0 + model.B]
+        m = xb.shape[0]
+        if m < model.B:
+            xb = t.cat([xb, t.zeros(model.B - m, 6, device=model.dev)])
+        model.set_inputs(xb)
+        out[c0:c0 + m] = model.forward()[:m].float().cpu().numpy()
+    return out
