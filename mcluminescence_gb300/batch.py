@@ -96,13 +96,15 @@ class BatchResult:
 class BernoulliBatch:
     """A packed batch resident on the GPU, ready to launch or replay."""
 
-    def __init__(self, specs: Sequence[SetSpec], *, precision: str = "fp32",
+    def __init__(self, specs: Optional[Sequence[SetSpec]], *, precision: str = "fp32",
                  rng: str = "philox", seed: int = 0, block: int = 256, ept: int = 4,
                  grid: int = 0, want_alive: bool = True, want_fates: bool = False,
-                 uniforms: Optional[np.ndarray] = None, device: str = "cuda"):
+                 uniforms: Optional[np.ndarray] = None, device: str = "cuda", packed=None):
+        """``specs`` (a list of SetSpec) or ``packed`` = (sets, segs, bin_offsets,
+        slot_offsets, u_offsets) host arrays as returned by ``pack_host``."""
         torch = _torch()
         self.lib = _lib.load()
-        self.specs = list(specs)
+        self.specs = list(specs) if specs is not None else None
         self.precision = _PREC[precision]
         self.rng = _RNG[rng]
         if self.precision == _lib.MCL_FP64 and block != 256:
@@ -110,7 +112,7 @@ class BernoulliBatch:
         if self.precision == _lib.MCL_FP64 and ept not in (1, 2):
             ept = 2
         self.block, self.ept, self.grid = int(block), int(ept), int(grid)
-        sets, segs, b_off, s_off, u_off = pack_host(self.specs)
+        sets, segs, b_off, s_off, u_off = packed if packed is not None else pack_host(self.specs)
         self.bin_offsets, self.slot_offsets, self.u_offsets = b_off, s_off, u_off
         self.n_bins_total = int(b_off[-1])
         self.n_slots_total = int(s_off[-1])
@@ -124,14 +126,16 @@ class BernoulliBatch:
                                            int(uniforms.size) if uniforms is not None else 0),
                    "mcl_b_validate")
         spi = self.block * self.ept
-        cap = int(sum(-(-sp.n_slots // spi) for sp in self.specs))
+        n_slots = sets["n_slots"].astype(np.int64)
+        cap = int(np.sum((n_slots + spi - 1) // spi))
         items = np.zeros(max(cap, 1), dtype=_lib.ITEM_DTYPE)
         n_items = self.lib.mcl_b_pack_items(_lib.ptr(sets), len(sets), spi, _lib.ptr(items), cap)
         if n_items < 0:
             _lib.check(int(n_items), "mcl_b_pack_items")
         self.n_items = int(n_items)
-        self.max_bins = int(max([sp.n_bins for sp in self.specs] or [0]))
+        self.max_bins = int(sets["n_bins"].max()) if len(sets) else 0
         self.host_sets, self.host_segs, self.host_items = sets, segs, items[:self.n_items]
+        self._trials = int(np.sum(n_slots * sets["total_steps"].astype(np.int64)))
         dev = torch.device(device)
         u8 = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).to(dev)
         self.d_sets = u8(sets) if len(sets) else torch.empty(8, dtype=torch.uint8, device=dev)
@@ -144,7 +148,7 @@ class BernoulliBatch:
         self.d_u = (torch.from_numpy(np.ascontiguousarray(uniforms[:n_u], dtype=np.float64)).to(dev)
                     if self.rng == _lib.MCL_RNG_INJECTED else None)
         self.d_status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.table_steps = int(sum(sp.total_steps for sp in self.specs))
+        self.table_steps = int(np.sum(sets["total_steps"]))
         self.ws_bytes = int(self.lib.mcl_b_workspace_size(_lib.ptr(sets), len(sets), self.precision))
         self.d_ws = torch.zeros(self.ws_bytes, dtype=torch.uint8, device=dev)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -217,7 +221,7 @@ class BernoulliBatch:
     @property
     def trials(self) -> int:
         """Electron-step trials of one run: sum over sets of slots x steps."""
-        return int(sum(sp.trials for sp in self.specs))
+        return self._trials
 
 
 def simulate_batch(specs: Sequence[SetSpec], **kw) -> BatchResult:

@@ -221,6 +221,20 @@ class SurrogateMLP:
                                          C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
                                          self.step_count, None, None, self._s()), "mcl_adam")
 
+    def state_dict(self) -> dict:
+        """FP32 master weights and biases (host tensors), for checkpoints."""
+        return {"W": [L.W.cpu() for L in self.layers], "b": [L.b.cpu() for L in self.layers],
+                "step": self.step_count}
+
+    def load_state_dict(self, st: dict) -> None:
+        t = self.torch
+        for L, W, b in zip(self.layers, st["W"], st["b"]):
+            L.W.copy_(W.to(self.dev))
+            L.b.copy_(b.to(self.dev))
+            L.Wb.copy_(L.W.to(t.bfloat16))
+            L.Wt.copy_(L.W.t().contiguous().to(t.bfloat16))
+        self.step_count = int(st.get("step", 0))
+
     def input_grad(self) -> "torch.Tensor":
         """d loss / d standardized input (after backward(want_input_grad=True))."""
         return self.dY[0][:, :6]
@@ -290,6 +304,31 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
         if log_every and (k % log_every == 0 or k == steps - 1):
             hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
     return hist
+
+
+def standardize_t(p):
+    """Device version of ``standardize`` (torch tensor [n][6])."""
+    import torch
+    lo = torch.tensor(LOW, dtype=p.dtype, device=p.device)
+    hi = torch.tensor(HIGH, dtype=p.dtype, device=p.device)
+    return 2.0 * (p - lo) / (hi - lo) - 1.0
+
+
+def predict_t(model: SurrogateMLP, params_t) -> "torch.Tensor":
+    """Predicted log curves for a device tensor of parameters [n][6] (float32
+    device tensor [n][200]); no host round trip."""
+    t = model.torch
+    X = standardize_t(params_t.float())
+    n = X.shape[0]
+    out = t.empty(n, DIMS[-1], dtype=t.float32, device=model.dev)
+    for c0 in range(0, n, model.B):
+        xb = X[c0:c0 + model.B]
+        m = xb.shape[0]
+        if m < model.B:
+            xb = t.cat([xb, t.zeros(model.B - m, 6, device=model.dev)])
+        model.set_inputs(xb)
+        out[c0:c0 + m] = model.forward()[:m]
+    return out
 
 
 def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
