@@ -32,6 +32,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
@@ -54,6 +56,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fit", action="store_true", help="skip the surrogate training / fitting measurement")
+    p.add_argument("--no-k", action="store_true", help="skip the event-driven kinetics measurement")
     p.add_argument("--fits", type=int, default=1024)
     p.add_argument("--plain-fits", type=int, default=128,
                    help="fits run with plain-MC DE (its per-fit cost does not depend on the batch)")
@@ -263,6 +266,8 @@ def main():
         "e2e": e2e, "gpu_launches": a.steps, "clocks": clk, "roofline": roof,
         "wall_s_timed": t_wall,
     }
+    if not a.no_k:
+        out["reference_kinetics"] = kinetics_k_bench(a, rank, world)
     if not a.no_fit:
         out["fitting"] = fitting_bench(a, rank)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -276,6 +281,70 @@ def main():
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def _esteps(res, params):
+    """Electron-steps of event-driven runs: sum over steps of the electrons
+    present at the step's start (what each step evaluates)."""
+    tot = 0.0
+    for j, rp in enumerate(params):
+        n = int(res.n_steps[j])
+        r = res.electron_ratio[:n, j] * rp.N_e
+        tot += rp.e0 + float(np.sum(r[:-1])) if n else 0.0
+    return tot
+
+
+def kinetics_k_bench(a, rank, world):
+    """Event-driven (reference) kinetics: the reference's default TL12
+    configuration through the drop-in simulate() (numpy's global stream, runs
+    in order), and 1,216 independent TL12-size simulations in parallel
+    (Philox); next to the CPU restatement of the same loop on one TL12 run."""
+    import numpy as np
+    import torch
+    from mcluminescence_gb300 import kinetics as K
+    from mcluminescence_gb300.config import default_config, initialize_runs
+    cfg = default_config()
+    np.random.seed(a.seed)
+    K.simulate(cfg)                               # warm-up (module load)
+    torch.cuda.synchronize()
+    np.random.seed(a.seed)
+    t0 = time.perf_counter()
+    (x_ax, lum, ratio, configs), res = K.simulate(cfg, return_result=True)
+    torch.cuda.synchronize()
+    compat_s = time.perf_counter() - t0
+    runs = initialize_runs(cfg)
+    params = [K.run_params(runs[r]) for r in runs for _ in range(int(cfg["exp_type_fp"]["sims"]))]
+    compat_esteps = _esteps(res, params)
+    # throughput: independent simulations of the TL12 rate-5 run, one CTA each
+    p5 = K.run_params(runs[2])
+    n_par = 8 * 152
+    K.run_kinetics([p5] * 8, 20000, rng="philox", seed=1, want_events=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rp, _ = K.run_kinetics([p5] * n_par, 20000, rng="philox", seed=a.seed, want_events=False)
+    torch.cuda.synchronize()
+    par_s = time.perf_counter() - t0
+    par_esteps = _esteps(rp, [p5] * n_par)
+    out = {"compat_tl12": {"config": "reference default (TL12 x basicTL12: 4 heating rates x 2 sims, "
+                                     "2000 traps, 3455 centres)", "seconds": compat_s,
+                           "steps": int(np.sum(res.n_steps)), "events": int(lum.sum()),
+                           "electron_steps": compat_esteps, "electron_steps_per_s": compat_esteps / compat_s},
+           "parallel_tl12_rate5": {"sims": n_par, "seconds": par_s, "electron_steps": par_esteps,
+                                   "electron_steps_per_s": par_esteps / par_s,
+                                   "events": int(rp.lum.sum())}}
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        from oracle import kinetics_k as ok
+        kr = ok.run_from_cfg(runs[3])          # the 20 K/s run (~1,200 steps)
+        st = ok.UniformStream(np.random.RandomState(a.seed))
+        t0 = time.perf_counter()
+        r = ok.run_sim(kr, st, 20000)
+        cpu_s = time.perf_counter() - t0
+        es = r.electron_ratio[:r.n_steps] * kr.N_e
+        cpu_esteps = int(kr.N_e * kr.e_ratio_start) + float(np.sum(es[:-1]))
+        out["cpu_port_one_run"] = {"seconds": cpu_s, "electron_steps_per_s": cpu_esteps / cpu_s, "cores": 1,
+                                   "kind": "port", "sample": "TL12 20 K/s run, oracle FP64 numpy "
+                                   "restatement (no dense distance matrix)"}
+    return out
 
 
 def fitting_bench(a, rank):

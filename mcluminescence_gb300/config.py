@@ -223,3 +223,19 @@ def initialize_runs(cfg: Any) -> Dict[int, Dict[str, Dict[str, Any]]]:
             run[name] = sr
         runs[i] = run
     return runs
+
+
+def default_config() -> Dict[str, Any]:
+    """The reference's default composition of conf/config_fp.yaml: experiment
+    group TL12 (conf/exp_type_fp/TL12.yaml) and physics group basicTL12
+    (conf/physics_fp/basicTL12.yaml), as plain dicts."""
+    return {
+        "exp_type_fp": {"name": "TL", "exp_type": "TL", "T_start": [0], "T_end": [1000],
+                        "T_rate": [0.1, 1, 5, 20], "duration": [8000, 800, 160, 40], "max_dt": 1,
+                        "sims": 2, "holes": 2000, "electrons": 1000, "N_e": 2000, "e_ratio_start": 1,
+                        "rho_prime": 3e-4, "boundary_factor": [1.2], "steps": 20000,
+                        "distance_plot": False, "x_lim": 800, "bin_size": 1},
+        "physics_fp": {"name": "basic", "alpha": 1.6e9, "b": 1e12, "k_b": 8.617343e-5,
+                       "E_loc_1": 1.2, "E_loc_2": 1.2, "E_cb": 1000, "D0": 400.35, "D": 0,
+                       "Retrap": 0.5, "s": 1e12},
+    }

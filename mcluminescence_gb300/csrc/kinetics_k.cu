@@ -63,6 +63,9 @@ __device__ __forceinline__ bool better(double v2, int i2, double v1, int i1) {
 
 struct Arrays {
   double *ex, *ey, *ez, *ed;  // electron coordinates, nearest distance
+  double* u2;                 // the step's wait uniform of each electron
+  float* edf;                 // nearest distance rounded to FP32 (kept in step with ed)
+  float* lw;                  // FP32 log-wait of the current step
   int32_t* en;                // nearest hole index
   uint8_t* choice;            // E_loc choice of the current step
   int32_t* mlist;             // electrons to rescan after a removal
@@ -72,9 +75,9 @@ struct Arrays {
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 __host__ __device__ inline size_t arrays_bytes(int e_cap, int h_cap) {
-  return align16(sizeof(double) * 4 * (size_t)e_cap) + align16(sizeof(int32_t) * (size_t)e_cap) +
-         align16((size_t)e_cap) + align16(sizeof(int32_t) * (size_t)e_cap) +
-         align16(sizeof(double) * 3 * (size_t)h_cap);
+  return align16(sizeof(double) * 5 * (size_t)e_cap) + align16(sizeof(float) * 2 * (size_t)e_cap) +
+         align16(sizeof(int32_t) * (size_t)e_cap) + align16((size_t)e_cap) +
+         align16(sizeof(int32_t) * (size_t)e_cap) + align16(sizeof(double) * 3 * (size_t)h_cap);
 }
 
 __device__ inline Arrays carve(unsigned char* base, int e_cap, int h_cap) {
@@ -84,7 +87,11 @@ __device__ inline Arrays carve(unsigned char* base, int e_cap, int h_cap) {
   A.ey = d + e_cap;
   A.ez = d + 2 * e_cap;
   A.ed = d + 3 * e_cap;
-  unsigned char* p = base + align16(sizeof(double) * 4 * (size_t)e_cap);
+  A.u2 = d + 4 * e_cap;
+  unsigned char* p = base + align16(sizeof(double) * 5 * (size_t)e_cap);
+  A.edf = reinterpret_cast<float*>(p);
+  A.lw = A.edf + e_cap;
+  p += align16(sizeof(float) * 2 * (size_t)e_cap);
   A.en = reinterpret_cast<int32_t*>(p);
   p += align16(sizeof(int32_t) * (size_t)e_cap);
   A.choice = p;
@@ -326,6 +333,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         }
       }
       A.ed[e] = bd;
+      A.edf[e] = __double2float_rn(bd);
       A.en[e] = bi;
     }
     __syncthreads();
@@ -353,9 +361,21 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       __syncthreads();
     }
     if (status != MCL_OK) break;
-    // waits: n uniforms, argmin and any()
-    double bv = INFINITY;
-    int bi = INT_MAX, any = 0;
+    // waits: n uniforms.  Pass 1 scores every electron with an FP32 log-wait
+    // log(-log(1-U)) - log(s e^{-E_cb/kT} + b e^{arg}) (absolute error < 5e-5,
+    // so a margin of 1e-3 in log space cannot exclude the FP64 minimum); pass 2
+    // evaluates the reference's FP64 wait exactly for the electrons within the
+    // margin of the FP32 minimum and takes np.argmin over them.  A non-finite
+    // FP32 score or a rate near FP64 over/underflow sends the whole step
+    // through the exact FP64 path.  wait != 0 (np.any) holds exactly when some
+    // log-wait is above -inf, as -inf means U == 0.
+    const float c1 = __double2float_rn(__ddiv_rn(-sm.E_loc_1, kT));
+    const float c2 = __double2float_rn(__ddiv_rn(-sm.E_loc_2, kT));
+    const float af = __double2float_rn(sm.alpha);
+    const float lb = __double2float_rn(log(sm.b));
+    const float lrcb = rcb > 0.0 ? __double2float_rn(log(rcb)) : -INFINITY;
+    float lmin = INFINITY;
+    int flags = 0;  // bit 0: exact path needed; bit 1: some wait is non-zero
     for (int c0 = 0; c0 < n_e; c0 += kChunk) {
       const int cnt = min(kChunk, n_e - c0);
       if (!ensure<BLOCK>(S, cnt)) {
@@ -364,24 +384,47 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       }
       for (int k = tid; k < cnt; k += BLOCK) {
         const int e = c0 + k;
-        const double E_loc = A.choice[e] ? sm.E_loc_2 : sm.E_loc_1;
-        const double arg = __dadd_rn(__ddiv_rn(-E_loc, kT), -__dmul_rn(sm.alpha, A.ed[e]));
-        const double rate = __dmul_rn(sm.b, exp(arg));
-        const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
-        const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -value(S, k))));
-        any |= (w != 0.0);
-        if (better(w, e, bv, bi)) {
-          bv = w;
-          bi = e;
-        }
+        const double u2 = value(S, k);
+        A.u2[e] = u2;
+        const float arg = (A.choice[e] ? c2 : c1) - af * A.edf[e];
+        const float lrt = lb + arg;
+        const float lrate = lrcb > -INFINITY ? fmaxf(lrcb, lrt) + log1pf(expf(-fabsf(lrcb - lrt))) : lrt;
+        const float E = -log1pf(-__double2float_rn(u2));
+        const float lw = logf(E) - lrate;
+        A.lw[e] = lw;
+        // FP64 over/underflow of the rate (life 0 or inf) is left to the exact path
+        if (isnan(lw) || lw == INFINITY || lrate > 700.0f || lrt < -700.0f || rcb == INFINITY) flags |= 1;
+        if (lw > -INFINITY) flags |= 2;
+        lmin = fminf(lmin, lw);
       }
       advance(S, cnt);
       __syncthreads();
     }
     if (status != MCL_OK) break;
+    double lmin_d;
+    int dummy_i, allflags;
+    block_argmin<BLOCK>(sh, (double)lmin, 0, flags, lmin_d, dummy_i, allflags);
+    const bool exact_all = (allflags & 1) != 0;
+    const float thr = (float)lmin_d + 1e-3f;
+    double bv = INFINITY;
+    int bi = INT_MAX, any = 0;
+    for (int e = tid; e < n_e; e += BLOCK) {
+      if (!exact_all && !(A.lw[e] <= thr)) continue;
+      const double E_loc = A.choice[e] ? sm.E_loc_2 : sm.E_loc_1;
+      const double arg = __dadd_rn(__ddiv_rn(-E_loc, kT), -__dmul_rn(sm.alpha, A.ed[e]));
+      const double rate = __dmul_rn(sm.b, exp(arg));
+      const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
+      const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -A.u2[e])));
+      any |= (w != 0.0);
+      if (better(w, e, bv, bi)) {
+        bv = w;
+        bi = e;
+      }
+    }
     double wmin;
     int emin;
     block_argmin<BLOCK>(sh, bv, bi, any, wmin, emin, any);
+    if (!exact_all) any = (allflags & 2) ? 1 : 0;
 
     // filling wait (tl_trap_lab.py:53-60)
     double lam;
@@ -435,6 +478,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         A.ey[n_e] = ney;
         A.ez[n_e] = nez;
         A.ed[n_e] = dn;
+        A.edf[n_e] = __double2float_rn(dn);
         A.en[n_e] = hn;
         A.hx[n_h] = nhx;
         A.hy[n_h] = nhy;
@@ -469,6 +513,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
         const int k = base + tid;
         double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
+        float f0 = 0;
         int n0 = 0;
         if (k < ne_tail) {
           const int s = e_idx + 1 + k;
@@ -476,6 +521,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
           y0 = A.ey[s];
           z0 = A.ez[s];
           d0 = A.ed[s];
+          f0 = A.edf[s];
           n0 = A.en[s];
         }
         if (k < nh_tail) {
@@ -491,6 +537,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
           A.ey[dst] = y0;
           A.ez[dst] = z0;
           A.ed[dst] = d0;
+          A.edf[dst] = f0;
           A.en[dst] = n0;
         }
         if (k < nh_tail) {
@@ -523,6 +570,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], dn, hn);
         if (tid == 0) {
           A.ed[e] = dn;
+          A.edf[e] = __double2float_rn(dn);
           A.en[e] = hn;
         }
         __syncthreads();

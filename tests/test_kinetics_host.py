@@ -33,3 +33,12 @@ def test_physics_keys_behave_like_the_dataclass():
     del bad["Retrap"]
     with pytest.raises(TypeError, match="missing 1 required"):
         physics(bad)
+
+
+def test_default_config_is_the_reference_composition():
+    import os
+    from mcluminescence_gb300.config import compose, default_config
+    conf = os.environ.get("MCL_REFERENCE_CONF", "/nonexistent")
+    if not os.path.isdir(conf):
+        pytest.skip("reference conf/ not available")
+    assert compose(conf) == default_config()
