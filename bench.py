@@ -266,6 +266,7 @@ def main():
         "e2e": e2e, "gpu_launches": a.steps, "clocks": clk, "roofline": roof,
         "wall_s_timed": t_wall,
     }
+    out["dose_fade_irsl"] = sequence_bench(a, rank)
     if not a.no_k:
         out["reference_kinetics"] = kinetics_k_bench(a, rank, world)
     if not a.no_fit:
@@ -281,6 +282,37 @@ def main():
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def sequence_bench(a, rank):
+    """2,048 irradiation -> ground-state fading -> IRSL sets (dose rate
+    U[0.05, 0.2] Gy/s to log-uniform 1..1000 Gy, D0 U[100, 500] Gy, 1e5 s of
+    fading in 200 geometric steps, 1,000 s of IR stimulation at 50 degC in 0.1 s
+    steps, sigma*Phi log-uniform 1e-3..1e-1 /s; traps start empty; uneven step
+    counts) replayed from one captured CUDA graph."""
+    import torch
+    from mcluminescence_gb300 import BernoulliBatch, schedule
+    specs = schedule.batch_dose_fade_irsl(2048, seed=a.seed + 1 + 977 * rank)
+    b = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=128, ept=8, want_alive=True)
+    st = torch.cuda.Stream()
+    b.capture(st)
+    for _ in range(2):
+        b.replay(st)
+    st.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record(st)
+    for _ in range(reps):
+        b.replay(st)
+    e1.record(st)
+    e1.synchronize()
+    if b.status() != 0:
+        raise RuntimeError(f"kernel status {b.status()}")
+    ms = e0.elapsed_time(e1) / reps
+    steps = [s.total_steps for s in specs]
+    return {"sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": ms,
+            "electron_steps_per_s": b.trials / (ms / 1e3), "steps_min": min(steps), "steps_max": max(steps),
+            "events_per_pass": int(b.result().lum.sum())}
 
 
 def _esteps(res, params):

@@ -168,3 +168,22 @@ def test_fill_fade_irsl_sequence_fp64():
     for i, (lum, alive, fates) in enumerate(oracle_all(specs, "f64", 8)):
         assert np.array_equal(res.lum_of(i), lum), i
         assert np.array_equal(res.alive_of(i), alive), i
+
+
+def test_fill_fade_irsl_sequence_fp32_fates():
+    """The filling path of the FP32 kernel (empty traps filled at the dose
+    rate, then fading and optical stimulation) against the oracle on the same
+    Philox integers."""
+    specs = schedule.batch_dose_fade_irsl(6, seed=9, n_min=200, n_max=900, fade_steps=30)
+    for s in specs:
+        s.segments[2] = schedule.optical(s.segments[2].rate_const, 200.0, 0.1, T_C=50.0,
+                                         bin_seconds=1.0)
+        s.finalize()
+    res = simulate_batch(specs, precision="fp32", seed=21, want_fates=True)
+    mism, ev = 0, 0
+    for i, (lum, alive, fates) in enumerate(oracle_all(specs, "f32", 21)):
+        mism += int(np.count_nonzero(res.fates_of(i) != fates))
+        ev += int(lum.sum())
+        assert abs(int(res.alive_of(i)[-1]) - int(alive[-1])) <= 2
+    assert ev > 100
+    assert mism <= 2
