@@ -297,3 +297,106 @@ def simulate_runs(runs, stream: UniformStream, steps: int, sims: int):
             ratio[:, j, ri] = res.electron_ratio
             results.append(res)
     return x_ax, lum, ratio, results
+
+
+# ---------------------------------------------------------------------------
+# lab-data objectives (src/class/tl_trap_lab.py:65-179)
+# ---------------------------------------------------------------------------
+def _lab_sim(r: KRun, stream: UniformStream, e_ratio: float):
+    rr = KRun(**{**r.__dict__, "e_ratio_start": float(e_ratio)})
+    return KSim(rr, stream)
+
+
+def _lab_step(sim: KSim, wait, tf):
+    """One iteration's event: pair creation when the fill wait is not longer
+    than the shortest recombination wait (min(dt_recomb, tf) keeps dt_recomb
+    on a tie, and dt == tf then picks the fill)."""
+    dt_recomb = np.min(wait) if wait.size else tf
+    dt = min(dt_recomb, tf)
+    if dt == tf:
+        sim.add_electron()
+        ev = (0, sim.electrons.shape[0] - 1, sim.holes.shape[0] - 1)
+    else:
+        e_idx = int(np.argmin(wait))
+        _, nearest = sim.nearest()
+        h_idx = int(nearest[e_idx])
+        sim.remove_pair(e_idx, h_idx)
+        ev = (1, e_idx, h_idx)
+    return dt, ev
+
+
+def tl_lab(r: KRun, stream: UniformStream, table: dict, D: float):
+    """TLTrapSim.TL_lab (tl_trap_lab.py:65-123): one fresh simulation per
+    table row, heating linearly from T_start to T_end over Duration with
+    filling at dose rate D; returns (mse, per-row final ratio, per-row events,
+    per-row draws)."""
+    n_rows = len(table["Duration"])
+    finals, events, draws, se = [], [], [], []
+    for k in range(n_rows):
+        start = stream.consumed
+        sim = _lab_sim(r, stream, table["e_ratio"][k])
+        T_start = table["T_start"][k] + 273.15
+        T_rate = (table["T_end"][k] - table["T_start"][k]) / table["Duration"][k]
+        wait = sim.recomb_wait(T_start)
+        tf = sim.filling_time(D)
+        t_cur, i, ev_log, ratio = 0.0, 0, [], None
+        while t_cur < table["Duration"][k]:
+            dt_recomb = np.min(wait) if wait.size else tf
+            dt = min(dt_recomb, tf)
+            T_now = T_start + T_rate * (t_cur + dt)
+            t_cur += dt
+            _, ev = _lab_step(sim, wait, tf)
+            ev_log.append((i,) + ev)
+            tf = sim.filling_time(D)
+            wait = sim.recomb_wait(T_now)
+            ratio = sim.electrons.shape[0] / r.N_e
+            i += 1
+        err = ratio - table["Fill"][k]
+        se.append(err ** 2)
+        finals.append(ratio)
+        events.append(np.array(ev_log, dtype=np.int64).reshape(-1, 4))
+        draws.append(stream.consumed - start)
+    return float(np.mean(se)), finals, events, draws
+
+
+def iso_lab(r: KRun, stream: UniformStream, table: dict):
+    """TLTrapSim.ISO_lab (tl_trap_lab.py:125-179): one simulation per
+    experiment number (sorted), held at its temperature with filling at its
+    dose rate, scored against e_ratio at each observation time; returns
+    (mse, per-experiment observed ratios, events, draws)."""
+    exp = np.asarray(table["exp_no"])
+    order = []
+    for v in exp:
+        if v not in order:
+            order.append(v)
+    se, obs_out, events, draws = [], [], [], []
+    for exp_no in sorted(order):
+        m = exp == exp_no
+        sub = {k: np.asarray(v)[m] for k, v in table.items()}
+        start = stream.consumed
+        sim = _lab_sim(r, stream, float(sub["e_ratio"][0]))
+        T_iso = float(sub["temp"][0]) + 273.15
+        D = float(sub["dose"][0])
+        wait = sim.recomb_wait(T_iso)
+        tf = sim.filling_time(D)
+        t_cur, i, ev_log, obs_idx, got = 0.0, 0, [], 0, []
+        obs = sub["time"]
+        while obs_idx < len(obs):
+            dt_recomb = np.min(wait) if wait.size else tf
+            dt = min(dt_recomb, tf)
+            t_cur += dt
+            _, ev = _lab_step(sim, wait, tf)
+            ev_log.append((i,) + ev)
+            tf = sim.filling_time(D)
+            wait = sim.recomb_wait(T_iso)
+            i += 1
+            while obs_idx < len(obs) and t_cur >= obs[obs_idx]:
+                fill = sim.electrons.shape[0] / r.N_e
+                target = sub["e_ratio"][sub["time"] == obs[obs_idx]][0]
+                se.append((fill - target) ** 2)
+                got.append(fill)
+                obs_idx += 1
+        obs_out.append(got)
+        events.append(np.array(ev_log, dtype=np.int64).reshape(-1, 4))
+        draws.append(stream.consumed - start)
+    return float(np.mean(se)), obs_out, events, draws

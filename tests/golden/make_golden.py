@@ -233,13 +233,68 @@ def run_box_ops(seed=123, n_ops=80):
             "box_ops/nearest": np.concatenate(nears).astype(np.int64)}
 
 
+# synthetic lab tables with the columns of data/processed/*.csv
+LAB_TL = {"Duration": [800.0, 1600.0, 2400.0, 3200.0, 1200.0, 2000.0],
+          "T_start": [300.0] * 6, "T_end": [275.0, 250.0, 225.0, 200.0, 290.0, 260.0],
+          "Fill": [0.05, 0.15, 0.30, 0.45, 0.10, 0.20], "e_ratio": [0.0, 0.0, 0.0, 0.0, 0.2, 0.0]}
+LAB_ISO = {"exp_no": [0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2],
+           "e_ratio": [0.0, 0.20, 0.35, 0.50, 0.0, 0.10, 0.20, 0.25, 0.3, 0.25, 0.2],
+           "temp": [15.0] * 4 + [120.0] * 4 + [200.0] * 3,
+           "dose": [0.092] * 4 + [0.092] * 4 + [0.05] * 3,
+           "time": [0.0, 500.0, 1000.0, 2500.0, 0.0, 300.0, 900.0, 1800.0, 0.0, 200.0, 600.0],
+           "L": [0.0] * 11}
+LAB_CFG = ["physics_fp=lab_TL", "exp_type_fp=TLlab", "physics_fp.E_loc_2=1.3",
+           "physics_fp.Retrap=0.4"]
+
+
+def run_lab(kind, seed):
+    import pandas as stub_pd
+    stub_pd.register_table("synthetic_tl", LAB_TL)
+    stub_pd.register_table("synthetic_iso", LAB_ISO)
+    cfg_plain = compose(CONF, LAB_CFG)
+    cfg = OmegaConf.create(cfg_plain)
+    runs = ref_engine.initialize_runs(cfg)
+    LOG["sims"] = []
+    _draws[0] = 0
+    np.random.seed(seed)
+    sim = ref_tl.TLTrapSim(runs[0])
+    init_draws = _draws[0]      # the constructor seeds a box before TL_lab re-initialises
+    LOG["sims"] = []
+    _draws[0] = 0
+    t0 = time.time()
+    mse = sim.TL_lab("synthetic_tl") if kind == "tl" else sim.ISO_lab("synthetic_iso")
+    wall = time.time() - t0
+    sims = LOG["sims"]
+    draws = []
+    for i, s in enumerate(sims):
+        end = sims[i + 1]["draw0"] if i + 1 < len(sims) else _draws[0]
+        draws.append(end - s["draw0"])
+    name = f"lab_{kind}"
+    table = LAB_TL if kind == "tl" else LAB_ISO
+    out = {f"{name}/cfg": np.frombuffer(json.dumps(cfg_plain).encode(), dtype=np.uint8),
+           f"{name}/table": np.frombuffer(json.dumps(table).encode(), dtype=np.uint8),
+           f"{name}/seed": np.array(seed), f"{name}/mse": np.array(mse),
+           f"{name}/n_sims": np.array(len(sims)), f"{name}/draws": np.array(draws, dtype=np.int64),
+           f"{name}/init_draws": np.array(init_draws)}
+    for i, s in enumerate(sims):
+        out[f"{name}/events{i}"] = np.array(s["events"], dtype=np.int64).reshape(-1, 4)
+    print(f"{name}: mse {mse:.6g}, {len(sims)} sims, events {[len(s['events']) for s in sims]}, "
+          f"draws {draws}, {wall:.1f}s", flush=True)
+    return out
+
+
 def main(argv):
-    names = argv[1:] or list(CASES) + ["box_ops"]
+    names = argv[1:] or list(CASES) + ["box_ops", "lab_tl", "lab_iso"]
     path = os.path.join(HERE, "kinetics_k.npz")
     data = dict(np.load(path)) if os.path.exists(path) else {}
     for n in names:
         data = {k: v for k, v in data.items() if not k.startswith(n + "/")}
-        data.update(run_box_ops() if n == "box_ops" else run_case(n, CASES[n]))
+        if n == "box_ops":
+            data.update(run_box_ops())
+        elif n in ("lab_tl", "lab_iso"):
+            data.update(run_lab(n[4:], seed=31 if n == "lab_tl" else 32))
+        else:
+            data.update(run_case(n, CASES[n]))
     np.savez_compressed(path, **data)
     print("wrote", path, os.path.getsize(path), "bytes")
 

@@ -1,14 +1,88 @@
-"""Stand-in for pandas: DataFrame.to_csv is a no-op (the reference writes its
-result table into its own read-only tree)."""
+"""Stand-in for the parts of pandas the reference's src/class touches.
+
+``DataFrame.to_csv`` is a no-op (the reference writes into its own read-only
+tree).  ``read_csv`` serves tables registered with ``register_table`` by the
+fixture generator (synthetic lab tables), so the reference's TL_lab / ISO_lab
+run unmodified on them.  The DataFrame supports what those methods use:
+``iterrows`` with attribute access, column attributes with ``mean``,
+``unique``, ``iloc`` and ``to_numpy``, and boolean row selection.
+"""
+import os
+
+import numpy as np
+
+_TABLES = {}
+
+
+def register_table(name, columns):
+    _TABLES[name] = {k: np.asarray(v) for k, v in columns.items()}
+
+
+class Series(np.ndarray):
+    def __new__(cls, a):
+        return np.asarray(a).view(cls)
+
+    @property
+    def iloc(self):
+        return _ILoc(self)
+
+    def unique(self):
+        out = []
+        for v in np.asarray(self):
+            if v not in out:
+                out.append(v)
+        return np.array(out)
+
+    def to_numpy(self):
+        return np.asarray(self).copy()
+
+    def mean(self, *a, **k):
+        return float(np.asarray(self).mean())
+
+
+class _ILoc:
+    def __init__(self, s):
+        self.s = s
+
+    def __getitem__(self, i):
+        return np.asarray(self.s)[i].item()
+
+
+class _Row:
+    def __init__(self, d):
+        self.__dict__.update(d)
 
 
 class DataFrame(dict):
     def __init__(self, data=None, columns=None):
-        super().__init__(data if isinstance(data, dict) else {})
+        super().__init__()
+        if isinstance(data, dict):
+            for k, v in data.items():
+                self[k] = np.asarray(v)
+
+    def __getattr__(self, k):
+        try:
+            return Series(self[k])
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+    def __getitem__(self, key):
+        if isinstance(key, (np.ndarray, Series)) and np.asarray(key).dtype == bool:
+            m = np.asarray(key)
+            return DataFrame({k: np.asarray(v)[m] for k, v in self.items()})
+        return dict.__getitem__(self, key)
+
+    def iterrows(self):
+        n = len(next(iter(self.values()))) if self else 0
+        for i in range(n):
+            yield i, _Row({k: np.asarray(v)[i].item() for k, v in self.items()})
 
     def to_csv(self, *a, **k):
         return None
 
 
-def read_csv(*a, **k):
-    raise NotImplementedError("lab-data objectives are not exercised by the fixtures")
+def read_csv(path, *a, **k):
+    name = os.path.splitext(os.path.basename(str(path)))[0]
+    if name not in _TABLES:
+        raise FileNotFoundError(path)
+    return DataFrame(dict(_TABLES[name]))

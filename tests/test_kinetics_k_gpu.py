@@ -10,7 +10,7 @@ from mcluminescence_gb300.config import initialize_runs
 pytestmark = pytest.mark.gpu
 
 DATA = load_k()
-CASES = [c for c in k_case_names(DATA) if c != "box_ops"]
+CASES = [c for c in k_case_names(DATA) if c not in ("box_ops", "lab_tl", "lab_iso")]
 
 
 def _check_against_golden(case, x_ax, lum, ratio, res):

@@ -8,7 +8,7 @@ from mcluminescence_gb300.config import initialize_runs
 from oracle import kinetics_k as ok
 
 DATA = load_k()
-CASES = [c for c in k_case_names(DATA) if c != "box_ops"]
+CASES = [c for c in k_case_names(DATA) if c not in ("box_ops", "lab_tl", "lab_iso")]
 FAST = CASES
 
 
@@ -65,3 +65,24 @@ def test_initialize_runs_divisibility():
                             "physics_fp": {"c": 5}})
     assert [r["exp_type_fp"]["b"] for r in runs.values()] == [7, 8, 7, 8]
     assert all(r["physics_fp"]["c"] == 5 for r in runs.values())
+
+
+@pytest.mark.parametrize("kind", ["tl", "iso"])
+def test_lab_objectives_match_reference(kind):
+    """TL_lab / ISO_lab restated: same MSE, event logs and draws as the
+    reference on synthetic lab tables (tl_trap_lab.py:65-179)."""
+    import json
+    name = f"lab_{kind}"
+    cfg = json.loads(bytes(DATA[f"{name}/cfg"]).decode())
+    table = json.loads(bytes(DATA[f"{name}/table"]).decode())
+    r = ok.run_from_cfg(initialize_runs(cfg)[0])
+    stream = ok.UniformStream(np.random.RandomState(int(DATA[f"{name}/seed"])))
+    stream.take(int(DATA[f"{name}/init_draws"]))
+    if kind == "tl":
+        mse, _, events, draws = ok.tl_lab(r, stream, table, D=float(cfg["physics_fp"]["D"]))
+    else:
+        mse, _, events, draws = ok.iso_lab(r, stream, table)
+    assert mse == float(DATA[f"{name}/mse"])
+    assert draws == list(DATA[f"{name}/draws"])
+    for i, ev in enumerate(events):
+        assert np.array_equal(ev, DATA[f"{name}/events{i}"])
