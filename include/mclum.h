@@ -134,6 +134,9 @@ typedef struct mcl_b_args {
 } mcl_b_args;
 
 /* ---- reference-kinetics (event-driven) mode ----------------------------- */
+#define MCL_LOOP_SIMULATE 0  /* simulate.py:51-92: waits, fill wait, dt cap, one event      */
+#define MCL_LOOP_LAB_TL 1    /* TL_lab (tl_trap_lab.py:90-108): heat until `duration`       */
+#define MCL_LOOP_LAB_ISO 2   /* ISO_lab (tl_trap_lab.py:147-172): until the last obs time  */
 /* One simulation: one (run, sim) pair of src/class/simulate.py:36-92, with
  * the run's parameters already read the way simulate.py:39-45 and
  * tl_trap_lab.py:27-43 read them (box sides computed on the host in FP64).  */
@@ -159,6 +162,9 @@ typedef struct mcl_k_sim {
   int64_t ws_offset;    /* bytes into the workspace (arrays in global memory) */
   int64_t ev_offset;    /* first event slot in events[] (4 int32 per event)   */
   int64_t ev_cap;       /* event slots of this simulation                     */
+  int32_t loop;         /* MCL_LOOP_*                                         */
+  int32_t n_obs;        /* MCL_LOOP_LAB_ISO: observation times                */
+  int64_t obs_offset;   /* first observation in obs_time[] / obs_ratio[]      */
 } mcl_k_sim;
 
 typedef struct mcl_k_args {
@@ -173,6 +179,8 @@ typedef struct mcl_k_args {
   int32_t* status;         /* [n_sims] 0 or a negative MCL_E* code            */
   const double* uniforms;  /* MCL_RNG_INJECTED                                 */
   uint32_t* mt_state;      /* MCL_RNG_MT19937: [625] key words + position, in/out */
+  const double* obs_time;  /* MCL_LOOP_LAB_ISO: observation times (s), ascending */
+  double* obs_ratio;       /* MCL_LOOP_LAB_ISO: electrons / N_e at each observation */
   void* workspace;         /* global-memory arrays when they exceed shared memory */
   int64_t workspace_bytes;
   uint64_t seed;           /* MCL_RNG_PHILOX key                               */

@@ -19,3 +19,6 @@ __all__ = [
 from .kinetics import run_kinetics, run_params, simulate, write_table  # noqa: F401,E402
 
 __all__ += ["simulate", "run_kinetics", "run_params", "write_table"]
+from .kinetics import TLTrapSim  # noqa: F401,E402
+
+__all__ += ["TLTrapSim"]

@@ -61,8 +61,13 @@ K_SIM_DTYPE = np.dtype(
                           "dose_rate", "T_start", "T_rate", "dt_cap", "duration", "N_e",
                           "L", "W", "H", "Lb", "Wb", "Hb")]
     + [(n, "<i4") for n in ("e0", "n_h0", "e_cap", "h_cap", "steps")] + [("stream_id", "<u4")]
-    + [(n, "<i8") for n in ("out_offset", "u_offset", "u_count", "ws_offset", "ev_offset", "ev_cap")],
+    + [(n, "<i8") for n in ("out_offset", "u_offset", "u_count", "ws_offset", "ev_offset", "ev_cap")]
+    + [("loop", "<i4"), ("n_obs", "<i4"), ("obs_offset", "<i8")],
     align=True)
+
+MCL_LOOP_SIMULATE = 0
+MCL_LOOP_LAB_TL = 1
+MCL_LOOP_LAB_ISO = 2
 
 
 class KArgs(C.Structure):
@@ -70,7 +75,8 @@ class KArgs(C.Structure):
         ("sims", C.c_void_p), ("x_ax", C.c_void_p), ("lum", C.c_void_p), ("ratio", C.c_void_p),
         ("events", C.c_void_p), ("n_events", C.c_void_p), ("n_steps", C.c_void_p),
         ("draws", C.c_void_p), ("status", C.c_void_p), ("uniforms", C.c_void_p),
-        ("mt_state", C.c_void_p), ("workspace", C.c_void_p), ("workspace_bytes", C.c_int64),
+        ("mt_state", C.c_void_p), ("obs_time", C.c_void_p), ("obs_ratio", C.c_void_p),
+        ("workspace", C.c_void_p), ("workspace_bytes", C.c_int64),
         ("seed", C.c_uint64), ("n_sims", C.c_int32), ("rng", C.c_int32), ("sequential", C.c_int32),
         ("block", C.c_int32), ("e_cap_max", C.c_int32), ("h_cap_max", C.c_int32),
         ("arrays_in_smem", C.c_int32), ("reserved", C.c_int32),

@@ -339,36 +339,28 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     __syncthreads();
   }
 
-  // ---- the step loop (simulate.py:51-92) ---------------------------------
+  // ---- block-collective pieces shared by the loops -------------------------
   const int64_t N = (int64_t)sm.N_e;
-  double t = 0.0;
-  int i = 0;
-  const int64_t out = sm.out_offset;
-  while (status == MCL_OK && t <= sm.duration) {
-    const double T = __dadd_rn(__dadd_rn(sm.T_start, __dmul_rn(sm.T_rate, t)), 273.15);
+  int n_ev_local = 0;
+  // Retrap choices and waits at temperature T (tl_trap_lab.py:48-51 with
+  // engine.py:65-77): 2n uniforms.  Pass 1 scores every electron with an FP32
+  // log-wait log(-log(1-U)) - log(s e^{-E_cb/kT} + b e^{arg}) (absolute error
+  // < 5e-5, so a margin of 1e-3 in log space cannot exclude the FP64 minimum);
+  // pass 2 evaluates the reference's FP64 wait exactly for the electrons within
+  // the margin of the FP32 minimum and takes np.argmin over them.  A
+  // non-finite FP32 score or a rate near FP64 over/underflow sends the whole
+  // step through the exact FP64 path.  wait != 0 (np.any) holds exactly when
+  // some log-wait is above -inf, as -inf means U == 0.
+  auto waits = [&](double T, double& wmin, int& emin, int& any) -> int {
     const double kT = __dmul_rn(sm.k_b, T);
     const double rcb = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT)));
-
-    // E_loc choices: n uniforms
     for (int c0 = 0; c0 < n_e; c0 += kChunk) {
       const int cnt = min(kChunk, n_e - c0);
-      if (!ensure<BLOCK>(S, cnt)) {
-        status = MCL_EBUDGET;
-        break;
-      }
+      if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
       for (int k = tid; k < cnt; k += BLOCK) A.choice[c0 + k] = value(S, k) < sm.Retrap ? 1 : 0;
       advance(S, cnt);
       __syncthreads();
     }
-    if (status != MCL_OK) break;
-    // waits: n uniforms.  Pass 1 scores every electron with an FP32 log-wait
-    // log(-log(1-U)) - log(s e^{-E_cb/kT} + b e^{arg}) (absolute error < 5e-5,
-    // so a margin of 1e-3 in log space cannot exclude the FP64 minimum); pass 2
-    // evaluates the reference's FP64 wait exactly for the electrons within the
-    // margin of the FP32 minimum and takes np.argmin over them.  A non-finite
-    // FP32 score or a rate near FP64 over/underflow sends the whole step
-    // through the exact FP64 path.  wait != 0 (np.any) holds exactly when some
-    // log-wait is above -inf, as -inf means U == 0.
     const float c1 = __double2float_rn(__ddiv_rn(-sm.E_loc_1, kT));
     const float c2 = __double2float_rn(__ddiv_rn(-sm.E_loc_2, kT));
     const float af = __double2float_rn(sm.alpha);
@@ -378,10 +370,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     int flags = 0;  // bit 0: exact path needed; bit 1: some wait is non-zero
     for (int c0 = 0; c0 < n_e; c0 += kChunk) {
       const int cnt = min(kChunk, n_e - c0);
-      if (!ensure<BLOCK>(S, cnt)) {
-        status = MCL_EBUDGET;
-        break;
-      }
+      if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
       for (int k = tid; k < cnt; k += BLOCK) {
         const int e = c0 + k;
         const double u2 = value(S, k);
@@ -400,14 +389,13 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       advance(S, cnt);
       __syncthreads();
     }
-    if (status != MCL_OK) break;
     double lmin_d;
     int dummy_i, allflags;
     block_argmin<BLOCK>(sh, (double)lmin, 0, flags, lmin_d, dummy_i, allflags);
     const bool exact_all = (allflags & 1) != 0;
     const float thr = (float)lmin_d + 1e-3f;
     double bv = INFINITY;
-    int bi = INT_MAX, any = 0;
+    int bi = INT_MAX, an = 0;
     for (int e = tid; e < n_e; e += BLOCK) {
       if (!exact_all && !(A.lw[e] <= thr)) continue;
       const double E_loc = A.choice[e] ? sm.E_loc_2 : sm.E_loc_1;
@@ -415,175 +403,225 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       const double rate = __dmul_rn(sm.b, exp(arg));
       const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
       const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -A.u2[e])));
-      any |= (w != 0.0);
+      an |= (w != 0.0);
       if (better(w, e, bv, bi)) {
         bv = w;
         bi = e;
       }
     }
-    double wmin;
-    int emin;
-    block_argmin<BLOCK>(sh, bv, bi, any, wmin, emin, any);
+    block_argmin<BLOCK>(sh, bv, bi, an, wmin, emin, any);
     if (!exact_all) any = (allflags & 2) ? 1 : 0;
+    return MCL_OK;
+  };
 
-    // filling wait (tl_trap_lab.py:53-60)
+  // filling wait (tl_trap_lab.py:53-60): one uniform whenever lambda > 0
+  auto fill_wait = [&](double& dt_fill) -> int {
     double lam;
     if ((int64_t)n_e == N || sm.dose_rate == 0.0) lam = 1e-20;
     else lam = __dmul_rn(__ddiv_rn(sm.dose_rate, sm.D0), (double)(N - (int64_t)n_e));
-    double dt_fill = 1e20;
+    dt_fill = 1e20;
     if (lam > 0.0) {
-      if (!ensure<BLOCK>(S, 1)) {
-        status = MCL_EBUDGET;
-        break;
-      }
+      if (!ensure<BLOCK>(S, 1)) return MCL_EBUDGET;
       dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -value(S, 0))));
       advance(S, 1);
     }
-    const double dt_recomb = any ? wmin : dt_fill;
-    double dt = dt_fill;  // Python's min(): the first minimal argument
-    if (dt_recomb < dt) dt = dt_recomb;
-    if (sm.dt_cap < dt) dt = sm.dt_cap;
-    t = __dadd_rn(t, dt);
-    if (i >= sm.steps) {  // x_ax[i] would raise IndexError (simulate.py:64)
-      status = MCL_EOVERFLOW;
-      break;
-    }
-    if (tid == 0) a.x_ax[out + i] = t;
-    double ev = 0.0;
+    return MCL_OK;
+  };
 
-    if (dt == dt_fill) {
-      // ---- pair creation (engine.py:133-152) ----
-      if (!ensure<BLOCK>(S, 6)) {
-        status = MCL_EBUDGET;
-        break;
+  auto log_event = [&](int step, int kind, int e, int h) {
+    if (tid == 0 && a.events && n_ev < sm.ev_cap) {
+      int32_t* evp = a.events + 4 * (sm.ev_offset + n_ev);
+      evp[0] = step;
+      evp[1] = kind;
+      evp[2] = e;
+      evp[3] = h;
+    }
+    ++n_ev;
+  };
+
+  // pair creation (engine.py:133-152)
+  auto pair_create = [&](int step) -> int {
+    if (!ensure<BLOCK>(S, 6)) return MCL_EBUDGET;
+    const double nex = __dmul_rn(value(S, 0), sm.L), ney = __dmul_rn(value(S, 1), sm.W),
+                 nez = __dmul_rn(value(S, 2), sm.H);
+    const double nhx = __dmul_rn(value(S, 3), sm.Lb), nhy = __dmul_rn(value(S, 4), sm.Wb),
+                 nhz = __dmul_rn(value(S, 5), sm.Hb);
+    advance(S, 6);
+    if (n_h == 0) return MCL_ENOHOLE;
+    if (n_e + 1 > sm.e_cap || n_h + 1 > sm.h_cap) return MCL_ECAPACITY;
+    double dn;
+    int hn;
+    nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, dn, hn);  // OLD holes only
+    if (tid == 0) {
+      A.ex[n_e] = nex;
+      A.ey[n_e] = ney;
+      A.ez[n_e] = nez;
+      A.ed[n_e] = dn;
+      A.edf[n_e] = __double2float_rn(dn);
+      A.en[n_e] = hn;
+      A.hx[n_h] = nhx;
+      A.hy[n_h] = nhy;
+      A.hz[n_h] = nhz;
+    }
+    log_event(step, 0, n_e, n_h);
+    ++n_e;
+    ++n_h;
+    __syncthreads();
+    return MCL_OK;
+  };
+
+  // recombination (engine.py:154-175)
+  auto remove_pair = [&](int step, int e_idx) -> int {
+    const int h_idx = A.en[e_idx];
+    __syncthreads();
+    log_event(step, 1, e_idx, h_idx);
+    // np.delete of electron row e_idx and hole h_idx: shift the tails down
+    const int ne_tail = n_e - 1 - e_idx, nh_tail = n_h - 1 - h_idx;
+    for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
+      const int k = base + tid;
+      double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
+      float f0 = 0;
+      int n0 = 0;
+      if (k < ne_tail) {
+        const int s = e_idx + 1 + k;
+        x0 = A.ex[s];
+        y0 = A.ey[s];
+        z0 = A.ez[s];
+        d0 = A.ed[s];
+        f0 = A.edf[s];
+        n0 = A.en[s];
       }
-      const double nex = __dmul_rn(value(S, 0), sm.L), ney = __dmul_rn(value(S, 1), sm.W),
-                   nez = __dmul_rn(value(S, 2), sm.H);
-      const double nhx = __dmul_rn(value(S, 3), sm.Lb), nhy = __dmul_rn(value(S, 4), sm.Wb),
-                   nhz = __dmul_rn(value(S, 5), sm.Hb);
-      advance(S, 6);
-      if (n_h == 0) {
-        status = MCL_ENOHOLE;
-        break;
+      if (k < nh_tail) {
+        const int s = h_idx + 1 + k;
+        hx0 = A.hx[s];
+        hy0 = A.hy[s];
+        hz0 = A.hz[s];
       }
-      if (n_e + 1 > sm.e_cap || n_h + 1 > sm.h_cap) {
-        status = MCL_ECAPACITY;
-        break;
+      __syncthreads();
+      if (k < ne_tail) {
+        const int dst = e_idx + k;
+        A.ex[dst] = x0;
+        A.ey[dst] = y0;
+        A.ez[dst] = z0;
+        A.ed[dst] = d0;
+        A.edf[dst] = f0;
+        A.en[dst] = n0;
       }
+      if (k < nh_tail) {
+        const int dst = h_idx + k;
+        A.hx[dst] = hx0;
+        A.hy[dst] = hy0;
+        A.hz[dst] = hz0;
+      }
+      __syncthreads();
+    }
+    --n_e;
+    --n_h;
+    if (tid == 0) sh.n_mask = 0;
+    __syncthreads();
+    for (int e = tid; e < n_e; e += BLOCK) {
+      int nn = A.en[e];
+      if (nn > h_idx) A.en[e] = --nn;
+      if (nn == h_idx) A.mlist[atomicAdd(&sh.n_mask, 1)] = e;
+    }
+    __syncthreads();
+    const int n_mask = sh.n_mask;
+    if (n_mask > 0 && n_h == 0) return MCL_ENOHOLE;
+    for (int m = 0; m < n_mask; ++m) {
+      const int e = A.mlist[m];
       double dn;
       int hn;
-      nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, dn, hn);  // OLD holes only
+      nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], dn, hn);
       if (tid == 0) {
-        A.ex[n_e] = nex;
-        A.ey[n_e] = ney;
-        A.ez[n_e] = nez;
-        A.ed[n_e] = dn;
-        A.edf[n_e] = __double2float_rn(dn);
-        A.en[n_e] = hn;
-        A.hx[n_h] = nhx;
-        A.hy[n_h] = nhy;
-        A.hz[n_h] = nhz;
-        if (a.events && n_ev < sm.ev_cap) {
-          int32_t* evp = a.events + 4 * (sm.ev_offset + n_ev);
-          evp[0] = i;
-          evp[1] = 0;
-          evp[2] = n_e;
-          evp[3] = n_h;
-        }
-      }
-      ++n_e;
-      ++n_h;
-      ++n_ev;
-      __syncthreads();
-    } else if (dt == dt_recomb) {
-      // ---- recombination (engine.py:154-175) ----
-      const int e_idx = emin;
-      const int h_idx = A.en[e_idx];
-      __syncthreads();
-      if (tid == 0 && a.events && n_ev < sm.ev_cap) {
-        int32_t* evp = a.events + 4 * (sm.ev_offset + n_ev);
-        evp[0] = i;
-        evp[1] = 1;
-        evp[2] = e_idx;
-        evp[3] = h_idx;
-      }
-      ++n_ev;
-      // np.delete of electron row e_idx and hole h_idx: shift the tails down
-      const int ne_tail = n_e - 1 - e_idx, nh_tail = n_h - 1 - h_idx;
-      for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
-        const int k = base + tid;
-        double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
-        float f0 = 0;
-        int n0 = 0;
-        if (k < ne_tail) {
-          const int s = e_idx + 1 + k;
-          x0 = A.ex[s];
-          y0 = A.ey[s];
-          z0 = A.ez[s];
-          d0 = A.ed[s];
-          f0 = A.edf[s];
-          n0 = A.en[s];
-        }
-        if (k < nh_tail) {
-          const int s = h_idx + 1 + k;
-          hx0 = A.hx[s];
-          hy0 = A.hy[s];
-          hz0 = A.hz[s];
-        }
-        __syncthreads();
-        if (k < ne_tail) {
-          const int dst = e_idx + k;
-          A.ex[dst] = x0;
-          A.ey[dst] = y0;
-          A.ez[dst] = z0;
-          A.ed[dst] = d0;
-          A.edf[dst] = f0;
-          A.en[dst] = n0;
-        }
-        if (k < nh_tail) {
-          const int dst = h_idx + k;
-          A.hx[dst] = hx0;
-          A.hy[dst] = hy0;
-          A.hz[dst] = hz0;
-        }
-        __syncthreads();
-      }
-      --n_e;
-      --n_h;
-      if (tid == 0) sh.n_mask = 0;
-      __syncthreads();
-      for (int e = tid; e < n_e; e += BLOCK) {
-        int nn = A.en[e];
-        if (nn > h_idx) A.en[e] = --nn;
-        if (nn == h_idx) A.mlist[atomicAdd(&sh.n_mask, 1)] = e;
+        A.ed[e] = dn;
+        A.edf[e] = __double2float_rn(dn);
+        A.en[e] = hn;
       }
       __syncthreads();
-      const int n_mask = sh.n_mask;
-      if (n_mask > 0 && n_h == 0) {
-        status = MCL_ENOHOLE;
+    }
+    return MCL_OK;
+  };
+
+  double t = 0.0;
+  int i = 0;
+  const int64_t out = sm.out_offset;
+  if (sm.loop == MCL_LOOP_SIMULATE) {
+    // ---- the step loop of simulate() (simulate.py:51-92) ------------------
+    while (status == MCL_OK && t <= sm.duration) {
+      const double T = __dadd_rn(__dadd_rn(sm.T_start, __dmul_rn(sm.T_rate, t)), 273.15);
+      double wmin, dt_fill;
+      int emin, any;
+      if ((status = waits(T, wmin, emin, any)) != MCL_OK) break;
+      if ((status = fill_wait(dt_fill)) != MCL_OK) break;
+      const double dt_recomb = any ? wmin : dt_fill;
+      double dt = dt_fill;  // Python's min(): the first minimal argument
+      if (dt_recomb < dt) dt = dt_recomb;
+      if (sm.dt_cap < dt) dt = sm.dt_cap;
+      t = __dadd_rn(t, dt);
+      if (i >= sm.steps) {  // x_ax[i] would raise IndexError (simulate.py:64)
+        status = MCL_EOVERFLOW;
         break;
       }
-      for (int m = 0; m < n_mask; ++m) {
-        const int e = A.mlist[m];
-        double dn;
-        int hn;
-        nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], dn, hn);
-        if (tid == 0) {
-          A.ed[e] = dn;
-          A.edf[e] = __double2float_rn(dn);
-          A.en[e] = hn;
-        }
-        __syncthreads();
+      if (tid == 0) a.x_ax[out + i] = t;
+      double ev = 0.0;
+      if (dt == dt_fill) {
+        if ((status = pair_create(i)) != MCL_OK) break;
+      } else if (dt == dt_recomb) {
+        if ((status = remove_pair(i, emin)) != MCL_OK) break;
+        ev = 1.0;
       }
-      ev = 1.0;
+      if (tid == 0) {
+        a.lum[out + i] = ev;
+        a.ratio[out + i] = __ddiv_rn((double)n_e, sm.N_e);
+      }
+      ++i;
+      if (sm.duration != 0.0 && t >= sm.duration) break;
     }
-    if (tid == 0) {
-      a.lum[out + i] = ev;
-      a.ratio[out + i] = __ddiv_rn((double)n_e, sm.N_e);
+  } else if (status == MCL_OK) {
+    // ---- the lab-data loops (tl_trap_lab.py:90-108 and :147-172) ----------
+    // T(t) = T_start[K] + T_rate (t + dt) after each event (isothermal: T_rate
+    // 0); waits and the fill wait are drawn before the loop and after every
+    // event; dt = min(dt_recomb, tf) with no cap; a simulation without
+    // electrons (.size == 0) waits for a pair creation.
+    const double T0 = __dadd_rn(sm.T_start, 273.15);
+    double wmin, tf;
+    int emin, any;
+    int obs_idx = 0;
+    if (sm.loop == MCL_LOOP_LAB_ISO && (!a.obs_time || !a.obs_ratio)) status = MCL_EINVAL;
+    if (status == MCL_OK) status = waits(T0, wmin, emin, any);
+    if (status == MCL_OK) status = fill_wait(tf);
+    while (status == MCL_OK) {
+      if (sm.loop == MCL_LOOP_LAB_TL ? !(t < sm.duration) : !(obs_idx < sm.n_obs)) break;
+      const double dt_recomb = n_e > 0 ? wmin : tf;
+      const double dt = tf < dt_recomb ? tf : dt_recomb;
+      const double T_now = __dadd_rn(T0, __dmul_rn(sm.T_rate, __dadd_rn(t, dt)));
+      t = __dadd_rn(t, dt);
+      if (i >= sm.steps) {
+        status = MCL_EOVERFLOW;
+        break;
+      }
+      if (tid == 0) a.x_ax[out + i] = t;
+      double ev = 0.0;
+      if (dt == tf) {
+        if ((status = pair_create(i)) != MCL_OK) break;
+      } else {
+        if ((status = remove_pair(i, emin)) != MCL_OK) break;
+        ev = 1.0;
+      }
+      if ((status = fill_wait(tf)) != MCL_OK) break;
+      if ((status = waits(T_now, wmin, emin, any)) != MCL_OK) break;
+      if (tid == 0) {
+        a.lum[out + i] = ev;
+        a.ratio[out + i] = __ddiv_rn((double)n_e, sm.N_e);
+      }
+      ++i;
+      while (obs_idx < sm.n_obs && t >= a.obs_time[sm.obs_offset + obs_idx]) {
+        if (tid == 0) a.obs_ratio[sm.obs_offset + obs_idx] = __ddiv_rn((double)n_e, sm.N_e);
+        ++obs_idx;
+      }
     }
-    ++i;
-    if (sm.duration != 0.0 && t >= sm.duration) break;
   }
+  (void)n_ev_local;
   if (tid == 0) {
     a.n_steps[si] = i;
     a.n_events[si] = n_ev;
@@ -660,6 +698,9 @@ extern "C" int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng
     const mcl_k_sim& s = sims[i];
     if (s.e0 < 0 || s.n_h0 < 0 || s.e_cap < s.e0 || s.h_cap < s.n_h0 || s.steps < 0) return MCL_EINVAL;
     if (s.ev_cap < 0 || s.ev_offset < 0 || s.out_offset < 0 || s.ws_offset < 0) return MCL_EINVAL;
+    if (s.loop < MCL_LOOP_SIMULATE || s.loop > MCL_LOOP_LAB_ISO || s.n_obs < 0 || s.obs_offset < 0)
+      return MCL_EINVAL;
+    if (s.loop == MCL_LOOP_LAB_ISO && s.n_obs == 0) return MCL_EINVAL;
     if (!(s.N_e > 0) || !std::isfinite(s.duration) || !std::isfinite(s.T_rate)) return MCL_EINVAL;
     if (rng == MCL_RNG_INJECTED && (s.u_offset < 0 || s.u_count < 0 || s.u_offset + s.u_count > n_uniforms))
       return MCL_ECAPACITY;

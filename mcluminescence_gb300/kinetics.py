@@ -82,6 +82,8 @@ class RunParams:
     Lb: float
     e0: int
     n_h0: int
+    loop: int = 0                 # MCL_LOOP_*
+    obs: Optional[np.ndarray] = None   # lab isothermal: observation times
 
 
 def run_params(run_cfg: Any, dose_rate: Optional[float] = None) -> RunParams:
@@ -116,6 +118,7 @@ class KResult:
     draws: np.ndarray
     status: np.ndarray
     events: List[np.ndarray]      # per simulation (n, 4): step, kind, e_idx, h_idx
+    obs_ratio: Optional[List[np.ndarray]] = None   # lab isothermal loop: ratio at each observation
 
 
 def _fill_sims(params: Sequence[RunParams], steps: int, extra: int):
@@ -137,6 +140,7 @@ def _fill_sims(params: Sequence[RunParams], steps: int, extra: int):
         r["out_offset"] = i * steps
         r["ev_offset"] = i * steps
         r["ev_cap"] = steps
+        r["loop"] = rp.loop
     return sims
 
 
@@ -176,6 +180,13 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
         if sequential:
             sims["u_offset"][0] = 0
             sims["u_count"][0] = n_u
+    obs_list = [np.asarray(rp.obs, dtype=np.float64) if rp.obs is not None else np.zeros(0) for rp in params]
+    n_obs_tot = int(sum(len(o) for o in obs_list))
+    off = 0
+    for i, o in enumerate(obs_list):
+        sims[i]["n_obs"] = len(o)
+        sims[i]["obs_offset"] = off
+        off += len(o)
     smem_flag, ws_need = C.c_int32(), C.c_int64()
     e_max, h_max = C.c_int32(), C.c_int32()
     ws_bytes = _ws_offsets(sims)
@@ -204,11 +215,16 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
         d_mt = torch.from_numpy(st.view(np.int32)).to(dev)
     d_ws = (torch.zeros(max(ws_bytes, 16), dtype=torch.uint8, device=dev)
             if not smem_flag.value else None)
+    d_obs_t = d_obs_r = None
+    if n_obs_tot:
+        d_obs_t = torch.from_numpy(np.concatenate(obs_list)).to(dev)
+        d_obs_r = torch.full((n_obs_tot,), float("nan"), dtype=torch.float64, device=dev)
     a = KArgs()
     a.sims, a.x_ax, a.lum, a.ratio = _lib.ptr(d_sims), _lib.ptr(x_ax), _lib.ptr(lum), _lib.ptr(ratio)
     a.events, a.n_events, a.n_steps = _lib.ptr(events), _lib.ptr(n_ev), _lib.ptr(n_st)
     a.draws, a.status, a.uniforms = _lib.ptr(draws), _lib.ptr(status), _lib.ptr(d_u)
     a.mt_state, a.workspace = _lib.ptr(d_mt), _lib.ptr(d_ws)
+    a.obs_time, a.obs_ratio = _lib.ptr(d_obs_t), _lib.ptr(d_obs_r)
     a.workspace_bytes = int(d_ws.numel()) if d_ws is not None else 0
     a.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     a.n_sims, a.rng, a.sequential, a.block = n, code, int(bool(sequential)), block
@@ -229,6 +245,10 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
             evs.append(None)
     res = KResult(x_ax.cpu().numpy().reshape(n, steps).T.copy(), lum.cpu().numpy().reshape(n, steps).T.copy(),
                   ratio.cpu().numpy().reshape(n, steps).T.copy(), nst, draws.cpu().numpy()[:n], st_h, evs)
+    if n_obs_tot:
+        o = d_obs_r.cpu().numpy()
+        res.obs_ratio = [o[int(sims[i]["obs_offset"]):int(sims[i]["obs_offset"]) + len(obs_list[i])]
+                         for i in range(n)]
     new_state = None
     if d_mt is not None:
         st = d_mt.cpu().numpy().view(np.uint32)
@@ -304,3 +324,113 @@ def write_table(path: str, lum: np.ndarray, ratio: np.ndarray) -> None:
             for s in range(sims):
                 for k in range(steps):
                     w.writerow([r, s, k, repr(float(lum[k, s, r])), repr(float(ratio[k, s, r]))])
+
+
+# ---------------------------------------------------------------------------
+# lab-data objectives: the TLTrapSim drop-in (tl_trap_lab.py:24-179)
+# ---------------------------------------------------------------------------
+def read_table(src) -> Dict[str, np.ndarray]:
+    """A lab table as columns: a dict of columns, or a CSV path (the reference
+    reads data/processed/<name>.csv with pandas)."""
+    if isinstance(src, dict):
+        return {k: np.asarray(v) for k, v in src.items()}
+    with open(src, newline="") as f:
+        rows = list(csv.DictReader(f))
+    out = {}
+    for k in rows[0].keys():
+        vals = [r[k] for r in rows]
+        try:
+            out[k] = np.array([float(v) for v in vals])
+        except ValueError:
+            out[k] = np.array(vals)
+    return out
+
+
+class TLTrapSim:
+    """GPU drop-in of src/class/tl_trap_lab.py:TLTrapSim for its lab objectives.
+
+    The constructor performs the reference's checks (``Physics(**physics_fp)``)
+    and, with ``rng="numpy"``, consumes the uniforms the reference's
+    constructor draws to seed its box (engine.py:124-129), so
+    ``np.random.seed(k); TLTrapSim(run).TL_lab(table)`` matches the reference.
+    ``TL_lab`` and ``ISO_lab`` take a lab table (dict of columns or a CSV path
+    with the reference's columns) and return the MSE like the reference.
+    """
+
+    def __init__(self, cfg: Any, *, e_ratio_start: Optional[float] = None, rng: str = "numpy",
+                 seed: Optional[int] = None, block: int = 256):
+        self.cfg = cfg
+        self.mc = cfg["exp_type_fp"]
+        self.phys = physics(cfg["physics_fp"])
+        self.D = _get(cfg["physics_fp"], "D", None)
+        self.rng, self.seed, self.block = rng, seed, block
+        self.last = None
+        e0 = int(self.mc["N_e"] * (e_ratio_start if e_ratio_start is not None else 0))
+        total_h = int(self.mc["holes"] * self.mc["boundary_factor"] ** 3)
+        if rng == "numpy":
+            if seed is not None:
+                np.random.seed(seed)
+            np.random.random_sample(3 * e0 + 3 * total_h)
+
+    def _params(self, e_ratio, T_start_C, T_rate, duration, D, loop, obs=None) -> RunParams:
+        run = {"exp_type_fp": dict(self.mc), "physics_fp": dict(self.cfg["physics_fp"])}
+        run["exp_type_fp"]["e_ratio_start"] = float(e_ratio)
+        run["physics_fp"].pop("dose_rate", None)
+        rp = run_params(run, dose_rate=0.0 if D is None else float(D))
+        rp.T_start, rp.T_rate, rp.duration, rp.dt_cap = float(T_start_C), float(T_rate), float(duration), 1e20
+        rp.loop = loop
+        rp.obs = obs
+        return rp
+
+    def _run(self, params, steps=4096):
+        while True:
+            if self.rng == "numpy":
+                state0 = np.random.get_state()
+                res, new_state = run_kinetics(params, steps, rng="mt19937", mt_state=state0, block=self.block)
+            else:
+                res, new_state = run_kinetics(params, steps, rng="philox", seed=self.seed or 0,
+                                              block=self.block)
+            if np.any(res.status == _lib.MCL_EOVERFLOW) and steps < 1 << 24:
+                steps *= 4        # more events than rows provisioned: run again with room
+                continue
+            break
+        if self.rng == "numpy":
+            np.random.set_state(("MT19937", new_state[1], new_state[2], state0[3], state0[4]))
+        _raise_for(res.status, steps)
+        self.last = res
+        return res
+
+    def TL_lab(self, table, *, plot: bool = False) -> float:
+        """tl_trap_lab.py:65-123: per row, heat from T_start to T_end over
+        Duration with filling at physics D; MSE of the final fill ratio."""
+        tb = read_table(table)
+        if self.D is None:
+            raise TypeError("unsupported operand type(s) for /: 'NoneType' and 'float'")
+        params = [self._params(tb["e_ratio"][k], tb["T_start"][k],
+                               (tb["T_end"][k] - tb["T_start"][k]) / tb["Duration"][k],
+                               tb["Duration"][k], self.D, _lib.MCL_LOOP_LAB_TL)
+                  for k in range(len(tb["Duration"]))]
+        res = self._run(params)
+        finals = np.array([res.electron_ratio[int(res.n_steps[j]) - 1, j] for j in range(len(params))])
+        self.finals = finals
+        return float(np.mean((finals - tb["Fill"]) ** 2))
+
+    def ISO_lab(self, table, *, plot: bool = False) -> float:
+        """tl_trap_lab.py:125-179: per experiment number, hold at its
+        temperature with filling at its dose rate; MSE over observation times."""
+        tb = read_table(table)
+        order = []
+        for v in tb["exp_no"]:
+            if v not in order:
+                order.append(v)
+        params, targets = [], []
+        for exp_no in sorted(order):
+            m = tb["exp_no"] == exp_no
+            sub = {k: v[m] for k, v in tb.items()}
+            obs = sub["time"].astype(np.float64)
+            params.append(self._params(sub["e_ratio"][0], sub["temp"][0], 0.0, 0.0, sub["dose"][0],
+                                       _lib.MCL_LOOP_LAB_ISO, obs))
+            targets.append(np.array([sub["e_ratio"][sub["time"] == o][0] for o in obs]))
+        res = self._run(params)
+        err = np.concatenate([r - tgt for r, tgt in zip(res.obs_ratio, targets)])
+        return float(np.mean(err ** 2))

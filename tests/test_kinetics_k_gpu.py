@@ -85,3 +85,40 @@ def test_philox_parallel_statistics_and_determinism():
     for r in range(3):
         m, s = got[:, r].mean(), got[:, r].std(ddof=1)
         assert abs(ref[:, r].mean() - m) < 4 * s + 1
+
+
+@pytest.mark.parametrize("kind", ["tl", "iso"])
+def test_lab_objectives_match_reference(kind):
+    """np.random.seed(k); TLTrapSim(run).TL_lab / ISO_lab on the GPU == the
+    reference on the same (synthetic) lab table."""
+    import json
+    from mcluminescence_gb300 import TLTrapSim
+    name = f"lab_{kind}"
+    cfg = json.loads(bytes(DATA[f"{name}/cfg"]).decode())
+    table = json.loads(bytes(DATA[f"{name}/table"]).decode())
+    np.random.seed(int(DATA[f"{name}/seed"]))
+    sim = TLTrapSim(initialize_runs(cfg)[0])
+    mse = sim.TL_lab(table) if kind == "tl" else sim.ISO_lab(table)
+    assert mse == float(DATA[f"{name}/mse"])
+    assert list(sim.last.draws) == list(DATA[f"{name}/draws"])
+    for i, ev in enumerate(sim.last.events):
+        assert np.array_equal(ev, DATA[f"{name}/events{i}"])
+
+
+def test_batched_lab_objective_and_optimizer():
+    """All DE candidates x lab rows in one launch; DE lowers the lab MSE."""
+    import json
+    from mcluminescence_gb300 import optimizer as O
+    cfg = json.loads(bytes(DATA["lab_tl/cfg"]).decode())
+    table = json.loads(bytes(DATA["lab_tl/table"]).decode())
+    run = initialize_runs(cfg)[0]
+    rng = np.random.default_rng(0)
+    lo = np.array([b[0] for b in O.DEFAULT_BOUNDS])
+    hi = np.array([b[1] for b in O.DEFAULT_BOUNDS])
+    cands = lo + (hi - lo) * rng.random((40, 10))
+    f1 = O.lab_objective_batch(run, cands, table, "tl", seed=5)
+    f2 = O.lab_objective_batch(run, cands, table, "tl", seed=5)
+    assert np.array_equal(f1, f2) and np.all(np.isfinite(f1))
+    best, mse, hist = O.optimize(run, table, "tl", gens=4, popsize=4, seed=1)
+    assert hist[-1] <= hist[0]
+    assert mse == hist[-1]
