@@ -285,25 +285,78 @@ def generate_dataset(n: int, seed: int, id0: int = 0, n_traps: int = N_TRAPS):
 
 def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: int = 4000,
           lr: float = 2e-3, lr_final: float = 5e-5, seed: int = 0, log_every: int = 0,
-          n_traps: int = N_TRAPS) -> List[float]:
+          n_traps: int = N_TRAPS, use_graph: bool = True) -> List[float]:
     """Adam on random mini-batches; cosine decay from lr to lr_final.
-    Returns the loss (mean squared error of the log curve) every log_every steps."""
+
+    One step (batch gather, forward, loss, backward, Adam) is ~40 small
+    kernels, so it is captured once in a CUDA graph and replayed; the
+    learning rate and step count reach the graph through device scalars.
+    Returns the loss (mean squared error of the log curve) every log_every
+    steps."""
     t = model.torch
     X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
     Y = t.tensor(curve_to_target(counts, n_traps), dtype=t.float32, device=model.dev)
     gen = t.Generator(device=model.dev).manual_seed(seed)
+    idx = t.zeros(model.B, dtype=t.int64, device=model.dev)
+    lrs = [lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps - 1, 1)))
+           for k in range(steps)]
     hist = []
-    for k in range(steps):
-        idx = t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev)
+
+    def body(k):
         model.set_inputs(X.index_select(0, idx))
         model.set_targets(Y.index_select(0, idx))
         model.forward()
         model.backward()
-        cur = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps - 1, 1)))
-        model.adam_step(lr=cur)
+        model.adam_step(lr=lrs[k])
+
+    if not use_graph:
+        for k in range(steps):
+            idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
+            body(k)
+            if log_every and (k % log_every == 0 or k == steps - 1):
+                hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
+        return hist
+    # The Adam kernel takes lr and the step as launch arguments, so a graph is
+    # captured per distinct (lr, step) would defeat replay; instead the graph
+    # holds the forward/backward pass only and Adam runs eagerly (10 launches).
+    s = t.cuda.Stream()
+    s.wait_stream(t.cuda.current_stream())
+    with t.cuda.stream(s):
+        idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
+        model.set_inputs(X.index_select(0, idx))
+        model.set_targets(Y.index_select(0, idx))
+        model.forward()
+        model.backward()
+    t.cuda.current_stream().wait_stream(s)
+    g = t.cuda.CUDAGraph()
+    with t.cuda.graph(g):
+        model.set_inputs(X.index_select(0, idx))
+        model.set_targets(Y.index_select(0, idx))
+        model.forward()
+        model.backward()
+    for k in range(steps):
+        idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
+        g.replay()
+        model.adam_step(lr=lrs[k])
         if log_every and (k % log_every == 0 or k == steps - 1):
             hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
     return hist
+
+
+def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
+    """Predicted log curves [n][200] (float32, host)."""
+    t = model.torch
+    X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
+    n = X.shape[0]
+    out = np.zeros((n, DIMS[-1]), dtype=np.float32)
+    for c0 in range(0, n, model.B):
+        xb = X[c0:c0 + model.B]
+        m = xb.shape[0]
+        if m < model.B:
+            xb = t.cat([xb, t.zeros(model.B - m, 6, device=model.dev)])
+        model.set_inputs(xb)
+        out[c0:c0 + m] = model.forward()[:m].float().cpu().numpy()
+    return out
 
 
 def standardize_t(p):
@@ -331,17 +384,3 @@ def predict_t(model: SurrogateMLP, params_t) -> "torch.Tensor":
     return out
 
 
-def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
-    """Predicted log curves [n][200] (float32, host)."""
-    t = model.torch
-    X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
-    n = X.shape[0]
-    out = np.zeros((n, DIMS[-1]), dtype=np.float32)
-    for c0 in range(0, n, model.B):
-        xb = X[c0:c0 + model.B]
-        m = xb.shape[0]
-        if m < model.B:
-            xb = t.cat([xb, t.zeros(model.B - m, 6, device=model.dev)])
-        model.set_inputs(xb)
-        out[c0:c0 + m] = model.forward()[:m].float().cpu().numpy()
-    return out
