@@ -120,6 +120,7 @@ def _declare(lib):
                                      C.POINTER(i32), C.POINTER(i32)]),
         "mcl_k_run": (C.c_int, [C.POINTER(KArgs), vp]),
         "mcl_gemm_nt": (C.c_int, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32, vp]),
+        "mcl_gemm_nt_tc": (C.c_int, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32, vp, vp]),
         "mcl_act_backward": (C.c_int, [i32, i32, vp, i32, vp, i32, i32, vp, i32, vp, i32, vp, vp]),
         "mcl_mse_loss": (C.c_int, [i32, i32, i32, vp, i32, vp, i32, C.c_float, vp, i32, vp, vp]),
         "mcl_adam": (C.c_int, [i32, i32, vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
@@ -140,7 +141,7 @@ EXPORTS = (
     "mcl_device_info", "mcl_b_validate", "mcl_b_pack_items", "mcl_b_workspace_size",
     "mcl_b_smem_bytes", "mcl_b_run", "mcl_b_graph_create", "mcl_graph_launch",
     "mcl_graph_destroy", "mcl_bench_philox", "mcl_b_run_static", "mcl_k_validate", "mcl_k_run",
-    "mcl_gemm_nt", "mcl_act_backward", "mcl_mse_loss", "mcl_adam", "mcl_f32_to_bf16",
+    "mcl_gemm_nt", "mcl_gemm_nt_tc", "mcl_act_backward", "mcl_mse_loss", "mcl_adam", "mcl_f32_to_bf16",
 )
 
 

@@ -6,10 +6,12 @@
 //
 // All GEMMs are "NT": C[m][n] = sum_k A[m][k] * B[n][k], both operands stored
 // with k contiguous (row-major A, and B as an out x in weight matrix like
-// torch.nn.Linear).  Tiles of 64 x 64 x 32 per CTA, four warps of 32 x 32,
-// mma.sync m16n8k16 BF16 tensor-core instructions fed by ldmatrix from padded
-// shared memory.  M and N must be multiples of 64, K a multiple of 32 (the
-// host pads 6 -> 32 inputs and 200 -> 256 outputs with zeros).
+// torch.nn.Linear).  Two implementations: gemm_nt_tc on the tcgen05 tensor
+// cores with the accumulator in tensor memory (used whenever the shape tiles
+// by 128 x 64 x 64, i.e. every GEMM of the surrogate at batch sizes that are
+// multiples of 128), and gemm_nt with mma.sync m16n8k16 instructions fed by
+// ldmatrix from padded shared memory (64 x 64 x 32 tiles) for other shapes.
+// The host pads 6 -> 64 inputs and 200 -> 256 outputs with zeros.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -200,6 +202,182 @@ __global__ void __launch_bounds__(256) f32_to_bf16(int64_t n, const float* __res
   for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) y[i] = __float2bfloat16_rn(x[i]);
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 path: the same NT GEMM on the 5th-generation tensor cores.
+// One CTA of 4 warps computes a 128 x NT tile.  Per 64-wide K slab the CTA
+// stages A (128 x 64) and B (NT x 64) in shared memory in the no-swizzle
+// K-major "core matrix" layout (8 rows x 16 bytes per core matrix, core
+// matrices adjacent along K 128 bytes apart, 8-row groups 1024 bytes apart),
+// one thread issues four tcgen05.mma (M = 128, N = NT, K = 16, BF16 inputs,
+// FP32 accumulator in tensor memory) and commits them to an mbarrier; the
+// epilogue reads the accumulator back with tcgen05.ld (warp w owns TMEM lanes
+// 32w..32w+31 = rows) and applies the same fused bias / GELU as gemm_nt.
+// Every mbarrier wait is bounded; on a timeout the kernel records an error
+// and still releases its tensor memory.
+// ---------------------------------------------------------------------------
+namespace tc {
+
+constexpr int kM = 128;   // rows per CTA (one tcgen05.mma M)
+constexpr int kKS = 64;   // K elements staged per slab
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (M/N) byte offsets >> 4, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  for (int i = 0; i < (1 << 20); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Copy rows [r0, r0 + rows) x K slab [k0, k0 + 64) of a k-contiguous bf16
+// matrix into the core-matrix layout.
+__device__ __forceinline__ void stage(unsigned char* dst, const __nv_bfloat16* src, int ld, int r0, int rows,
+                                      int k0) {
+  for (int c = threadIdx.x; c < rows * (kKS / 8); c += blockDim.x) {
+    const int r = c / (kKS / 8), kc = c % (kKS / 8);
+    const uint4 v = *reinterpret_cast<const uint4*>(&src[(size_t)(r0 + r) * ld + k0 + kc * 8]);
+    *reinterpret_cast<uint4*>(dst + ((r >> 3) * (kKS / 8) + kc) * 128 + (r & 7) * 16) = v;
+  }
+}
+
+template <int EPI, int NT>
+__global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+                                                  const __nv_bfloat16* __restrict__ B, int ldb,
+                                                  const float* __restrict__ bias, float* __restrict__ C, int ldc,
+                                                  __nv_bfloat16* __restrict__ Y, int ldy,
+                                                  __nv_bfloat16* __restrict__ Yt, int ldyt, int32_t* err) {
+  __shared__ __align__(1024) unsigned char sA[kM * kKS * 2];
+  __shared__ __align__(1024) unsigned char sB[NT * kKS * 2];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kM, n0 = blockIdx.x * NT;
+  const uint32_t mbar_a = smem_u32(&mbar);
+  if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), NT);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+  constexpr uint32_t idesc = idesc_bf16(kM, NT);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < K; k0 += kKS) {
+    stage(sA, A, lda, m0, kM, k0);
+    stage(sB, B, ldb, n0, NT, k0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      fence_after();
+#pragma unroll
+      for (int kk = 0; kk < kKS / 16; ++kk) {
+        const uint64_t ad = sdesc(smem_u32(sA) + kk * 256, 128, 1024);
+        const uint64_t bd = sdesc(smem_u32(sB) + kk * 256, 128, 1024);
+        mma(tmem, ad, bd, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
+      }
+      commit(mbar_a);
+    }
+    __syncwarp();
+    const bool got = mbar_wait(mbar_a, phase);
+    ok = __syncthreads_and(got ? 1 : 0) != 0;   // every thread leaves the loop together
+    phase ^= 1;
+    fence_after();
+    if (!ok) break;
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    const int m = m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      float v[16];
+      ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int n = n0 + c0 + j;
+        float x = v[j];
+        if (EPI != EPI_F32) x += bias[n];
+        C[(size_t)m * ldc + n] = x;
+        if (EPI == EPI_BIAS_GELU) {
+          const __nv_bfloat16 y = __float2bfloat16_rn(gelu(x));
+          Y[(size_t)m * ldy + n] = y;
+          if (Yt) Yt[(size_t)n * ldyt + m] = y;
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, NT);
+  (void)M;
+  (void)N;
+}
+
+}  // namespace tc
+
 }  // namespace
 }  // namespace mcl
 
@@ -271,6 +449,31 @@ extern "C" int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream)
   if (n == 0) return MCL_OK;
   const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
   f32_to_bf16<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(n, x, reinterpret_cast<__nv_bfloat16*>(y));
+  MCL_CUDA_TRY(cudaGetLastError());
+  return MCL_OK;
+}
+
+extern "C" int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
+                              const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
+                              int32_t ldy, void* Yt, int32_t ldyt, int32_t* err, void* stream) {
+  constexpr int NT = 64;
+  if (M <= 0 || N <= 0 || K <= 0 || M % tc::kM || N % NT || K % tc::kKS) return MCL_EINVAL;
+  if (!A || !B || !C || !err || lda < K || ldb < K || ldc < N || (lda % 8) || (ldb % 8)) return MCL_EINVAL;
+  if (((uintptr_t)A | (uintptr_t)B) & 15) return MCL_EINVAL;
+  if (epilogue != EPI_F32 && !bias) return MCL_EINVAL;
+  if (epilogue == EPI_BIAS_GELU && (!Y || ldy < N || (Yt && ldyt < M))) return MCL_EINVAL;
+  dim3 grid(N / NT, M / tc::kM);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const auto* a = reinterpret_cast<const __nv_bfloat16*>(A);
+  const auto* b = reinterpret_cast<const __nv_bfloat16*>(B);
+  auto* y = reinterpret_cast<__nv_bfloat16*>(Y);
+  auto* yt = reinterpret_cast<__nv_bfloat16*>(Yt);
+  switch (epilogue) {
+    case EPI_F32: tc::gemm_nt_tc<EPI_F32, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
+    case EPI_BIAS: tc::gemm_nt_tc<EPI_BIAS, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
+    case EPI_BIAS_GELU: tc::gemm_nt_tc<EPI_BIAS_GELU, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
+    default: return MCL_EINVAL;
+  }
   MCL_CUDA_TRY(cudaGetLastError());
   return MCL_OK;
 }

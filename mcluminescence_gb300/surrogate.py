@@ -142,6 +142,8 @@ class SurrogateMLP:
         self.dZ = [bf(B, n) for n in self.outs]
         self.dZt = [bf(n, B) for n in self.outs]
         self.loss = f32(1)
+        self.tc_err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.use_tcgen05 = True
         self.step_count = 0
 
     # -- plumbing -------------------------------------------------------------
@@ -153,9 +155,19 @@ class SurrogateMLP:
         return C.c_void_p(t.data_ptr()) if t is not None else None
 
     def _gemm(self, epi, M, N, K, A, lda, Bm, ldb, bias, Cm, ldc, Y=None, ldy=0, Yt=None, ldyt=0):
-        _lib.check(self.lib.mcl_gemm_nt(epi, M, N, K, self._p(A), lda, self._p(Bm), ldb, self._p(bias),
-                                        self._p(Cm), ldc, self._p(Y), ldy, self._p(Yt), ldyt, self._s()),
-                   "mcl_gemm_nt")
+        """tcgen05 GEMM (tensor-memory accumulator) when the shape tiles by
+        128 x 64 x 64, the mma.sync kernel otherwise."""
+        args = (epi, M, N, K, self._p(A), lda, self._p(Bm), ldb, self._p(bias), self._p(Cm), ldc,
+                self._p(Y), ldy, self._p(Yt), ldyt)
+        if self.use_tcgen05 and M % 128 == 0 and N % 64 == 0 and K % 64 == 0:
+            _lib.check(self.lib.mcl_gemm_nt_tc(*args, self._p(self.tc_err), self._s()), "mcl_gemm_nt_tc")
+        else:
+            _lib.check(self.lib.mcl_gemm_nt(*args, self._s()), "mcl_gemm_nt")
+
+    def check_errors(self) -> None:
+        """Raise if a tcgen05 completion wait timed out in any launch so far."""
+        if int(self.tc_err.item()):
+            raise RuntimeError("tcgen05 GEMM: a completion wait timed out")
 
     # -- data -----------------------------------------------------------------
     def set_inputs(self, x_std: "torch.Tensor") -> None:
@@ -340,6 +352,7 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
         model.adam_step(lr=lrs[k])
         if log_every and (k % log_every == 0 or k == steps - 1):
             hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
+    model.check_errors()
     return hist
 
 

@@ -36,10 +36,12 @@ def test_gemm_nt_matches_torch(epi, M, N, K):
         assert torch.equal(Yt, gy.t().contiguous())
 
 
-def test_gradients_match_float64_reference():
+@pytest.mark.parametrize("tcgen05", [True, False])
+def test_gradients_match_float64_reference(tcgen05):
     import torch
     from mcluminescence_gb300 import surrogate as S
     m = S.SurrogateMLP(batch=256, seed=3)
+    m.use_tcgen05 = tcgen05
     rng = np.random.default_rng(0)
     x = S.standardize(S.sample_params(256, rng))
     y = rng.normal(-2.0, 0.5, (256, 200)).astype(np.float32)
@@ -48,6 +50,7 @@ def test_gradients_match_float64_reference():
     out = m.forward().float().cpu().numpy()
     m.backward()
     torch.cuda.synchronize()
+    m.check_errors()
     loss_ref, gW, gb, out_ref = S.reference_forward_backward(m, x, y)
     assert np.abs(out - out_ref).max() < 0.05 * np.abs(out_ref).max()
     loss_gpu = float(m.loss.item()) / (256 * 200)
@@ -104,3 +107,38 @@ def test_training_learns_monte_carlo_curves():
     big = Ch > 20
     ratio = np.sqrt(np.mean((pred[big] - Ch[big]) ** 2 / Ch[big]))
     assert ratio < 4.0, ratio
+
+
+@pytest.mark.parametrize("epi", [0, 1, 2])
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 256, 256), (4096, 64, 256), (256, 64, 4096)])
+def test_gemm_tcgen05_matches_torch(epi, M, N, K):
+    """The tcgen05 / tensor-memory GEMM against torch and against the mma.sync kernel."""
+    import torch
+    lib = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(7 * M + N + K + epi)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    bias = torch.randn(N, device="cuda", generator=g)
+    outs = []
+    for fn in ("mcl_gemm_nt_tc", "mcl_gemm_nt"):
+        Cm = torch.full((M, N), float("nan"), device="cuda")
+        Y = torch.zeros(M, N, dtype=torch.bfloat16, device="cuda")
+        Yt = torch.zeros(N, M, dtype=torch.bfloat16, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        p = lambda t: C.c_void_p(t.data_ptr())
+        args = [epi, M, N, K, p(A), K, p(B), K, p(bias), p(Cm), N, p(Y), N, p(Yt), M]
+        rc = getattr(lib, fn)(*args, p(err), s) if fn.endswith("_tc") else getattr(lib, fn)(*args, s)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        outs.append((Cm, Y, Yt))
+    ref = A.float() @ B.float().t()
+    if epi:
+        ref = ref + bias
+    Cm, Y, Yt = outs[0]
+    torch.testing.assert_close(Cm, ref, rtol=1e-4, atol=1e-3 * K ** 0.5)
+    torch.testing.assert_close(Cm, outs[1][0], rtol=1e-4, atol=1e-3 * K ** 0.5)
+    if epi == 2:
+        assert torch.equal(Yt, Y.t().contiguous())
+        assert (Y.float() - torch.nn.functional.gelu(Cm).to(torch.bfloat16).float()).abs().max() == 0
