@@ -35,43 +35,49 @@ def _torch():
 
 
 def pack_host(specs: Sequence[SetSpec]):
-    """Host struct arrays for ``specs``: (sets, segs, n_bins_total, n_slots_total,
-    bin_offsets, slot_offsets, u_offsets, n_uniforms)."""
+    """Host struct arrays for ``specs``: (sets, segs, bin_offsets, slot_offsets,
+    u_offsets).  Column-wise numpy assignment, so packing thousands of sets
+    costs milliseconds."""
     n_sets = len(specs)
-    n_segs = int(sum(len(s.segments) for s in specs))
+    for sp in specs:
+        sp.finalize()
+    seg_counts = np.array([len(sp.segments) for sp in specs], dtype=np.int64)
+    n_segs = int(seg_counts.sum())
     sets = np.zeros(n_sets, dtype=_lib.SET_DTYPE)
     segs = np.zeros(n_segs, dtype=_lib.SEG_DTYPE)
-    b_off = np.zeros(n_sets + 1, dtype=np.int64)
-    s_off = np.zeros(n_sets + 1, dtype=np.int64)
-    u_off = np.zeros(n_sets + 1, dtype=np.int64)
-    g = 0
-    t_off = 0
-    for i, sp in enumerate(specs):
-        sp.finalize()
-        rec = sets[i]
-        rec["n_slots"] = sp.n_slots
-        rec["n_filled"] = sp.n_filled
-        rec["seg_begin"] = g
-        rec["seg_count"] = len(sp.segments)
-        rec["n_bins"] = sp.n_bins
-        rec["set_id"] = sp.set_id & 0xFFFFFFFF
-        rec["bin_offset"] = b_off[i]
-        rec["slot_offset"] = s_off[i]
-        rec["u_offset"] = u_off[i]
-        rec["total_steps"] = sp.total_steps
-        rec["step_offset"] = t_off
-        t_off += sp.total_steps
-        rec["E"], rec["s"], rec["alpha"], rec["k_b"] = sp.E, sp.s, sp.alpha, sp.k_b
-        for sg in sp.segments:
-            r = segs[g]
-            r["n_steps"], r["steps_per_bin"], r["bin_offset"] = sg.n_steps, sg.steps_per_bin, sg.bin_offset
-            r["flags"] = _lib.MCL_SEG_THERMAL if sg.thermal else 0
-            r["dt"], r["dt_growth"], r["T0"], r["beta"] = sg.dt, sg.dt_growth, sg.T0, sg.beta
-            r["rate_const"], r["fill_rate"] = sg.rate_const, sg.fill_rate
-            g += 1
-        b_off[i + 1] = b_off[i] + sp.n_bins
-        s_off[i + 1] = s_off[i] + sp.n_slots
-        u_off[i + 1] = u_off[i] + sp.n_slots * (1 + sp.total_steps)
+    all_segs = [sg for sp in specs for sg in sp.segments]
+    if n_segs:
+        col = lambda name, dt: np.fromiter((getattr(sg, name) for sg in all_segs), dtype=dt, count=n_segs)
+        segs["n_steps"] = col("n_steps", np.int32)
+        segs["steps_per_bin"] = col("steps_per_bin", np.int32)
+        segs["bin_offset"] = col("bin_offset", np.int32)
+        segs["flags"] = np.where(col("thermal", bool), _lib.MCL_SEG_THERMAL, 0)
+        for name in ("dt", "dt_growth", "T0", "beta", "rate_const", "fill_rate"):
+            segs[name] = col(name, np.float64)
+    seg_steps = segs["n_steps"].astype(np.int64)
+    seg_bins = -(-seg_steps // np.maximum(segs["steps_per_bin"].astype(np.int64), 1))
+    seg_begin = np.concatenate([[0], np.cumsum(seg_counts)[:-1]]) if n_sets else np.zeros(0, np.int64)
+    owner = np.repeat(np.arange(n_sets), seg_counts)
+    total_steps = np.bincount(owner, weights=seg_steps, minlength=n_sets).astype(np.int64)
+    n_bins = np.bincount(owner, weights=seg_bins, minlength=n_sets).astype(np.int64)
+    sc = lambda name, dt: np.fromiter((getattr(sp, name) for sp in specs), dtype=dt, count=n_sets)
+    n_slots = sc("n_slots", np.int64)
+    sets["n_slots"] = n_slots
+    sets["n_filled"] = sc("n_filled", np.int64)
+    sets["seg_begin"] = seg_begin
+    sets["seg_count"] = seg_counts
+    sets["n_bins"] = n_bins
+    sets["set_id"] = sc("set_id", np.int64) & 0xFFFFFFFF
+    b_off = np.concatenate([[0], np.cumsum(n_bins)]).astype(np.int64)
+    s_off = np.concatenate([[0], np.cumsum(n_slots)]).astype(np.int64)
+    u_off = np.concatenate([[0], np.cumsum(n_slots * (1 + total_steps))]).astype(np.int64)
+    sets["bin_offset"] = b_off[:-1]
+    sets["slot_offset"] = s_off[:-1]
+    sets["u_offset"] = u_off[:-1]
+    sets["total_steps"] = total_steps
+    sets["step_offset"] = np.concatenate([[0], np.cumsum(total_steps)[:-1]]) if n_sets else 0
+    for name in ("E", "s", "alpha", "k_b"):
+        sets[name] = sc(name, np.float64)
     return sets, segs, b_off, s_off, u_off
 
 
