@@ -22,15 +22,17 @@
 // * the CTA copies 256-step chunks of (c_j, q_j) into shared memory;
 // * FP32 mode spends 16 random bits per electron-step in the common case: a
 //   Philox block (four 32-bit words) covers 8 steps of a slot.  The step's
-//   16-bit field h becomes f = 1 + h 2^-16 with one logic op (a byte permute
-//   first for the upper four steps); d = (f - K) - c w (an FADD and an FFMA,
-//   K = 1 + 2^-21).  d >= 0 proves u >= c w >= p, so nothing happens.  The
-//   sign bits of all slots of a step are OR-ed and one branch per step enters
-//   the exact test, which draws the uniform's low 16 bits from a separate
-//   Philox counter and checks u32 < ceil(p 2^32), p = -expm1f(-c w); it runs
-//   with probability ~ c w + 2^-16.  Halving the Philox work per trial this
-//   way matters because the 32x32->64 multiplies of the Philox rounds occupy
-//   the FMA-heavy pipe, the kernel's binding unit;
+//   16-bit field h becomes the float 2^23 + h with one byte permute, and one
+//   FFMA gives d = 2^23 + h - c16 w (c16 = c 2^16 from the step table);
+//   d >= 2^23 + 1 proves u >= p, so nothing happens.  Each step keeps the
+//   minimum d over the thread's slots (3-input min).  In segments without
+//   filling one branch per 8-step block enters the exact test, which draws
+//   the uniform's low 16 bits from a separate Philox counter and checks
+//   u32 < ceil(p 2^32), p = -expm1f(-c w); it runs with probability
+//   ~ c w + 2^-16 per trial.  Filling segments branch once per step (a refill
+//   changes the next step's test).  Per trial the fast path is one byte
+//   permute, one FFMA and half a min, next to 1/8 of a Philox call (20
+//   32x32->64 multiplies on the FMA-heavy pipe, 20 3-input XORs);
 // * events are added to shared-memory bins (rare); at each bin end the warp
 //   sums the filled-trap counts with one reduction; when an item ends the CTA
 //   adds every non-zero bin to HBM with one atomic.
@@ -178,19 +180,47 @@ __device__ __forceinline__ uint32_t word_of(const uint4& r, int q) {
   return q == 0 ? r.x : (q == 1 ? r.y : (q == 2 ? r.z : r.w));
 }
 
-// Step t (0..7) of a Philox block uses a 16-bit field h of word t&3: bits
-// 22..7 of the word for t < 4, bits 22..7 of the word rotated by 16 for t >= 4.
-// fast_f returns 1 + h * 2^-16 by dropping the field into a float's mantissa.
+// Step t (0..7) of a Philox block uses the 16-bit field h of word t&3: the
+// word's upper half for t < 4, its lower half for t >= 4.  field_f returns the
+// float 2^23 + h with one byte permute (h becomes the low mantissa bits under
+// the exponent of 2^23).
 template <int T>
-__device__ __forceinline__ float fast_f(uint32_t word) {
-  const uint32_t x = (T < 4) ? word : __byte_perm(word, 0, 0x1032);
-  return __uint_as_float((x & 0x007fff80u) | 0x3f800000u);
+__device__ __forceinline__ float field_f(uint32_t word) {
+  return __uint_as_float(__byte_perm(word, 0x4B000000u, (T < 4) ? 0x7432 : 0x7410));
 }
 
 template <int T>
 __device__ __forceinline__ uint32_t field16(uint32_t word) {
-  const uint32_t x = (T < 4) ? word : __byte_perm(word, 0, 0x1032);
-  return (x >> 7) & 0xffffu;
+  return (T < 4) ? (word >> 16) : (word & 0xffffu);
+}
+
+// Fast test of the FP32 mode.  The shared-memory step table holds
+// c16 = c * 2^16 and q16 = q * 2^16 (exact power-of-two scalings).  For a
+// filled trap d = fl(2^23 + h - c16 w) (one FFMA), for an empty trap of a
+// filling segment d = fl(2^23 + h - q16).  An event needs u32 < ceil(p 2^32)
+// with u32 = h 2^16 + lo16, hence h < p 2^16 <= c16 w (1 + 2^-21) < c16 w + 2^-5
+// when c w < 1, so the exact value of d is below 2^23 + 2^-5 and d rounds to
+// at most 2^23; d >= kCand = 2^23 + 1 therefore proves that nothing happens.
+// (For c w >= 1, d <= 2^23 + 65535 - 65536 and the trial is always a
+// candidate.)  The test admits h <= c16 w + 1/2, i.e. about c w + 2^-16 of the
+// trials, which go to the exact test.
+constexpr float kCand = 8388609.0f;  // 2^23 + 1
+constexpr float kInv16 = 0x1p-16f;
+
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+template <int N>
+__device__ __forceinline__ float min_all(const float (&d)[N]) {
+  float m = d[0];
+  int i = 1;
+#pragma unroll
+  for (; i + 1 < N; i += 2) m = min3f(m, d[i], d[i + 1]);
+  if (i < N) m = fminf(m, d[i]);
+  return m;
 }
 
 // Per-thread state of the FP32 kernel for one work item.
@@ -201,40 +231,41 @@ struct SlotState {
   uint32_t filled;     // bit i: slot i holds an electron
 };
 
-// One step (index T within its Philox block) for all EPT slots.
-template <int EPT, bool FILL, int T>
-__device__ __forceinline__ void step_f32(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                         const uint4 (&r)[EPT], float c, float qf, int64_t kstep,
-                                         uint32_t* s_lum, int bin, float alpha) {
-  constexpr float kMargin = 1.0f + 0x1p-21f;
+// Exact test of slot i at step T of the block for a trap that is filled.
+template <int EPT, int T>
+__device__ __forceinline__ bool try_escape(const KParams& P, const mcl_set& st, SlotState<EPT>& S, int i,
+                                           uint32_t word, float c16, int64_t kstep, uint32_t* s_lum, int bin) {
+  const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
+  if (!escape_exact(u32, c16 * kInv16, S.w[i])) return false;
+  S.filled &= ~(1u << i);
+  S.w[i] = 0.0f;
+  atomicAdd(&s_lum[bin], 1u);
+  if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)kstep;
+  return true;
+}
+
+// One step of a filling segment (index T within its Philox block) for all
+// EPT slots: filled traps may escape, empty ones may be refilled.
+template <int EPT, int T>
+__device__ __forceinline__ void step_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                          const uint4 (&r)[EPT], float c16, float q16, int64_t kstep,
+                                          uint32_t* s_lum, int bin, float alpha) {
   float d[EPT];
-  uint32_t any = 0;
 #pragma unroll
   for (int i = 0; i < EPT; ++i) {
-    const float fk = fast_f<T>(word_of(r[i], T & 3)) - kMargin;
-    if (FILL && !((S.filled >> i) & 1u)) {
-      d[i] = fk - qf;
-    } else {
-      d[i] = __fmaf_rn(-c, S.w[i], fk);
-    }
-    any |= __float_as_uint(d[i]);
+    const float f = field_f<T>(word_of(r[i], T & 3));
+    d[i] = ((S.filled >> i) & 1u) ? __fmaf_rn(-c16, S.w[i], f) : __fsub_rn(f, q16);
   }
-  if ((int32_t)any < 0) {
+  if (min_all<EPT>(d) < kCand) {
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
-      if ((int32_t)__float_as_uint(d[i]) < 0) {
-        const uint32_t h = field16<T>(word_of(r[i], T & 3));
+      if (d[i] < kCand) {
+        const uint32_t word = word_of(r[i], T & 3);
         if ((S.filled >> i) & 1u) {
-          const uint32_t u32 = full_u32(h, (uint32_t)kstep, S.slot[i], st.set_id, P);
-          if (escape_exact(u32, c, S.w[i])) {
-            S.filled &= ~(1u << i);
-            S.w[i] = 0.0f;
-            atomicAdd(&s_lum[bin], 1u);
-            if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)kstep;
-          }
-        } else if (FILL && S.slot[i] < (uint32_t)st.n_slots) {
-          const uint32_t u32 = full_u32(h, (uint32_t)kstep, S.slot[i], st.set_id, P);
-          if (threshold_exact(u32, qf)) {
+          try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin);
+        } else if (S.slot[i] < (uint32_t)st.n_slots) {
+          const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
+          if (threshold_exact(u32, q16 * kInv16)) {
             const uint4 rr = philox_ks((uint32_t)kstep, S.slot[i], st.set_id, kTagRefill, P);
             S.w[i] = refill_w(rr.x, alpha);
             S.filled |= 1u << i;
@@ -245,29 +276,112 @@ __device__ __forceinline__ void step_f32(const KParams& P, const mcl_set& st, Sl
   }
 }
 
-// The steps of one Philox block (8 steps; fewer at a segment's end when
-// FULL is false) starting at chunk index jq.
-template <int EPT, bool FILL, bool FULL>
-__device__ __forceinline__ void block_f32(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                          uint32_t blk, const float* s_c, const float* s_q, int jq,
-                                          int nq, int64_t kstep, uint32_t* s_lum, uint32_t* s_alive,
-                                          int& bin, int& to_flush, int spb, int remaining_after,
-                                          float alpha) {
+// The steps of one Philox block of a filling segment (8 steps; fewer at the
+// segment's end when FULL is false), one branch per step.
+template <int EPT, bool FULL>
+__device__ __forceinline__ void block_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                           uint32_t blk, const float* s_c, const float* s_q, int jq,
+                                           int nq, int64_t kstep, uint32_t* s_lum, uint32_t* s_alive,
+                                           int& bin, int& to_flush, int spb, int remaining_after,
+                                           float alpha) {
   uint4 r[EPT];
 #pragma unroll
   for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-#define MCL_STEP(T)                                                                              \
-  if (FULL || (T) < nq) {                                                                        \
-    step_f32<EPT, FILL, T>(P, st, S, r, s_c[jq + (T)], FILL ? s_q[jq + (T)] : 0.0f, kstep + (T), \
-                           s_lum, bin, alpha);                                                   \
-    if (--to_flush == 0) {                                                                       \
-      if (s_alive) warp_flush((uint32_t)__popc(S.filled), &s_alive[bin]);                        \
-      ++bin;                                                                                     \
-      to_flush = min(spb, remaining_after - (T));                                                \
-    }                                                                                            \
+#define MCL_STEP(T)                                                                             \
+  if (FULL || (T) < nq) {                                                                       \
+    step_fill<EPT, T>(P, st, S, r, s_c[jq + (T)], s_q[jq + (T)], kstep + (T), s_lum, bin, alpha); \
+    if (--to_flush == 0) {                                                                      \
+      if (s_alive) warp_flush((uint32_t)__popc(S.filled), &s_alive[bin]);                       \
+      ++bin;                                                                                    \
+      to_flush = min(spb, remaining_after - (T));                                               \
+    }                                                                                           \
   }
   MCL_STEP(0) MCL_STEP(1) MCL_STEP(2) MCL_STEP(3) MCL_STEP(4) MCL_STEP(5) MCL_STEP(6) MCL_STEP(7)
 #undef MCL_STEP
+}
+
+// Escape candidates of step T of a non-filling block (entered only when the
+// step's minimum d is below kCand).  dcount gains 1 << 4T per escape.
+template <int EPT, int T>
+__device__ __forceinline__ void escapes_of_step(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                                const uint4 (&r)[EPT], float c16, int64_t kstep,
+                                                uint32_t* s_lum, int bin, uint32_t& dcount) {
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    uint32_t word = word_of(r[i], T & 3);
+    // Recompute d here rather than keep the fast pass's 8 x EPT values live.
+    asm volatile("" : "+r"(word));
+    if (((S.filled >> i) & 1u) && __fmaf_rn(-c16, S.w[i], field_f<T>(word)) < kCand) {
+      if (try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin)) dcount += 1u << (4 * T);
+    }
+  }
+}
+
+// The steps of one Philox block of a segment without filling.  Traps only
+// empty here, so a d computed before an escape earlier in the block can only
+// over-report candidates: the fast pass evaluates d for all 8 steps, keeps
+// each step's minimum, and one branch per block enters the exact tests.  The
+// bin bookkeeping runs afterwards for the whole block: alive counts at bin
+// ends inside the block subtract the escapes up to that step, which dcount
+// holds as 4-bit counts per step (prefix sums by one multiply; EPT <= 8
+// keeps every nibble below 16).
+template <int EPT, bool FULL>
+__device__ __forceinline__ void block_nofill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                             uint32_t blk, const float* s_c, int jq, int nq, int64_t kstep,
+                                             uint32_t* s_lum, uint32_t* s_alive, int& bin, int& to_flush,
+                                             int spb, int seg_left) {
+  static_assert(EPT <= 8, "per-step escape counts are 4-bit fields");
+  uint4 r[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
+  const float4 ca = *reinterpret_cast<const float4*>(s_c + jq);
+  const float4 cb = *reinterpret_cast<const float4*>(s_c + jq + 4);
+  const float c16[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+  float m[8];
+#define MCL_MIN(T)                                                              \
+  if (FULL || (T) < nq) {                                                       \
+    float d[EPT];                                                               \
+    _Pragma("unroll") for (int i = 0; i < EPT; ++i)                             \
+        d[i] = __fmaf_rn(-c16[T], S.w[i], field_f<T>(word_of(r[i], (T) & 3)));  \
+    m[T] = min_all<EPT>(d);                                                     \
+  } else {                                                                      \
+    m[T] = kCand;                                                               \
+  }
+  MCL_MIN(0) MCL_MIN(1) MCL_MIN(2) MCL_MIN(3) MCL_MIN(4) MCL_MIN(5) MCL_MIN(6) MCL_MIN(7)
+#undef MCL_MIN
+  const uint32_t alive0 = (uint32_t)__popc(S.filled);
+  uint32_t dcount = 0;
+  if (min_all<8>(m) < kCand) {
+#define MCL_SLOW(T)                                                                           \
+  if ((FULL || (T) < nq) && m[T] < kCand) {                                                   \
+    int b = bin;                                                                              \
+    for (int tf = to_flush; (T) >= tf; tf += spb) ++b;                                        \
+    escapes_of_step<EPT, T>(P, st, S, r, c16[T], kstep + (T), s_lum, b, dcount);             \
+  }
+    MCL_SLOW(0) MCL_SLOW(1) MCL_SLOW(2) MCL_SLOW(3) MCL_SLOW(4) MCL_SLOW(5) MCL_SLOW(6) MCL_SLOW(7)
+#undef MCL_SLOW
+  }
+  const int n = FULL ? 8 : nq;
+  if (to_flush > n) {
+    to_flush -= n;
+    return;
+  }
+  const uint32_t cum = dcount * 0x11111111u;  // nibble t: escapes in steps 0..t
+  int t = to_flush - 1;                        // block step that ends the current bin
+  for (;;) {
+    if (s_alive) warp_flush(alive0 - ((cum >> (4 * t)) & 0xfu), &s_alive[bin]);
+    ++bin;
+    const int next = min(spb, seg_left - t - 1);
+    if (next == 0) {  // the segment's last step
+      to_flush = 0;
+      return;
+    }
+    if (t + next >= n) {
+      to_flush = t + next - n + 1;
+      return;
+    }
+    t += next;
+  }
 }
 
 // One segment of one work item (FP32).
@@ -284,20 +398,28 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
     __syncthreads();
     for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
       const float2 cq = tab[j0 + jj];
-      s_c[jj] = cq.x;
-      s_q[jj] = cq.y;
+      s_c[jj] = __fmul_rn(cq.x, 65536.0f);
+      s_q[jj] = __fmul_rn(cq.y, 65536.0f);
     }
     __syncthreads();
     int jq = 0;
     for (; jq + 8 <= nj; jq += 8) {
-      block_f32<EPT, FILL, true>(P, st, S, bbase + (uint32_t)((j0 + jq) >> 3), s_c, s_q, jq, 8,
-                                 kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
-                                 sg.n_steps - (j0 + jq) - 1, alpha);
+      const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
+      if (FILL)
+        block_fill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush,
+                              spb, sg.n_steps - (j0 + jq) - 1, alpha);
+      else
+        block_nofill<EPT, true>(P, st, S, blk, s_c, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
+                                sg.n_steps - (j0 + jq));
     }
     if (jq < nj) {  // the segment's last, partial Philox block
-      block_f32<EPT, FILL, false>(P, st, S, bbase + (uint32_t)((j0 + jq) >> 3), s_c, s_q, jq, nj - jq,
-                                  kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
-                                  sg.n_steps - (j0 + jq) - 1, alpha);
+      const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
+      if (FILL)
+        block_fill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
+                               to_flush, spb, sg.n_steps - (j0 + jq) - 1, alpha);
+      else
+        block_nofill<EPT, false>(P, st, S, blk, s_c, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
+                                 to_flush, spb, sg.n_steps - (j0 + jq));
     }
   }
 }

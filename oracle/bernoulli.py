@@ -35,10 +35,10 @@ segments, local step j of segment g of slot e draws from
                       (2(j&1), 2(j&1)+1) of philox(P_g + (j>>1), e, set_id,
                       TAG_STEP), P_g = sum of ceil(n_steps/2); FP64 mode.
 ``layout="f32"``      Philox4x32-10, eight steps per call: step j takes the
-                      16-bit field h = bits 22..7 of word t&3 of
+                      16-bit field h of word t&3 of
                       philox(P_g + (j>>3), e, set_id, TAG_STEP), t = j&7,
-                      P_g = sum of ceil(n_steps/8); for t >= 4 the word's two
-                      16-bit halves are swapped first.  The uniform is
+                      P_g = sum of ceil(n_steps/8): the word's upper half
+                      for t < 4, its lower half for t >= 4.  The uniform is
                       u32 = (h << 16) | lo16 with lo16 the low 16 bits of word
                       0 of philox(k, e, set_id, TAG_LOW) (k = the set's global
                       step); an event happens iff u32 < p * 2^32.  The
@@ -152,9 +152,7 @@ class _Draws:
                 self._blk_id = b
             t = j & 7
             word = self._blk[t & 3]
-            if t >= 4:
-                word = ((word << np.uint64(16)) | (word >> np.uint64(16))) & np.uint64(0xFFFFFFFF)
-            h = (word >> np.uint64(7)) & np.uint64(0xFFFF)
+            h = (word >> np.uint64(16)) if t < 4 else (word & np.uint64(0xFFFF))
             u = h.astype(np.float64) * 2.0 ** -16
             cand = np.nonzero(u < thr)[0]
             if cand.size:
