@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--seed", type=int, default=20261203)
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--ept", type=int, default=0)
+    p.add_argument("--occupancy", type=int, default=0,
+                   help="register-capped FP32 build (resident CTAs per SM it targets; 0 = default)")
     p.add_argument("--sets", type=int, default=N_SETS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -171,11 +173,11 @@ def main():
     specs = schedule.batch_tl_iso(a.sets, seed=a.seed + 7919 * rank)
     for s in specs:
         s.set_id += rank * a.sets
-    block, ept = a.block, a.ept
+    block, ept, occ = a.block, a.ept, a.occupancy
     if not block or not ept:
-        block, ept = autotune.pick_bernoulli(specs, precision="fp32")
+        block, ept, occ = autotune.pick_bernoulli(specs, precision="fp32")
     batch = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=block, ept=ept,
-                           want_alive=True)
+                           want_alive=True, occupancy=occ)
     stream = torch.cuda.Stream()
     batch.capture(stream)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -219,12 +221,12 @@ def main():
     # ---- end to end through the public API (host specs in, host bins out) ----
     e2e = None
     if not a.no_e2e:
-        res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept)
+        res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, occupancy=occ)
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(a.steps):
-            res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept)
+            res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, occupancy=occ)
         torch.cuda.synchronize()
         barrier()
         e2e_s = (time.perf_counter() - t0) / a.steps
@@ -260,7 +262,7 @@ def main():
                                "(150-300 C, 1e4 s, dt 1 s)",
                    "sets_per_gpu": a.sets, "traps_per_gpu": int(sum(s.n_slots for s in specs)),
                    "trials_per_step_per_gpu": int(trials), "precision": "fp32",
-                   "rng": "philox4x32-10", "block": block, "ept": ept, "n_items": batch.n_items,
+                   "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ, "n_items": batch.n_items,
                    "l2": "flushed between passes (256 MB write, untimed)",
                    "parallelism": f"replicas x{world} (independent sets, no collective)"},
         "e2e": e2e, "gpu_launches": a.steps, "clocks": clk, "roofline": roof,

@@ -130,7 +130,10 @@ typedef struct mcl_b_args {
   int32_t ept;             /* slots per thread: 1, 2, 4 or 8                    */
   int32_t grid;            /* persistent CTAs; 0 = SM count x occupancy         */
   int32_t zero_outputs;    /* 1: clear lum/alive/fates/status before the launch */
-  int32_t reserved;
+  int32_t occupancy;       /* FP32 build: 0 = default; else resident CTAs per
+                              SM the build targets (fewer registers): 4 at
+                              block 256 / 8 at block 128 with ept 2, 3 at
+                              block 256 / 6 at block 128 with ept 4           */
 } mcl_b_args;
 
 /* ---- reference-kinetics (event-driven) mode ----------------------------- */

@@ -1,6 +1,7 @@
 """Launch-shape autotuner for the Bernoulli kernel.
 
-Times each (threads per CTA, traps per thread) candidate with CUDA events on a
+Times each (threads per CTA, traps per thread, register-capped build)
+candidate with CUDA events on a
 deterministic sample of the batch (every 32nd set, so the ragged size and step
 mix is kept) and caches the winner per (device, precision, shape bucket) in a
 JSON file next to the library.
@@ -16,8 +17,9 @@ from . import build as _build
 from .schedule import SetSpec
 
 CANDIDATES = {
-    "fp32": [(256, 4), (256, 2), (128, 4), (128, 2), (256, 8), (128, 8)],
-    "fp64": [(256, 1), (256, 2)],
+    "fp32": [(256, 4, 0), (256, 2, 0), (128, 4, 0), (128, 2, 0), (256, 8, 0), (128, 8, 0),
+             (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)],
+    "fp64": [(256, 1, 0), (256, 2, 0)],
 }
 CACHE = os.path.join(_build.LIBDIR, "autotune.json")
 
@@ -39,10 +41,11 @@ def _load():
         return {}
 
 
-def time_shape(specs, precision, block, ept, reps=2) -> float:
+def time_shape(specs, precision, block, ept, occupancy=0, reps=2) -> float:
     import torch
     from .batch import BernoulliBatch
-    b = BernoulliBatch(specs, precision=precision, seed=1, block=block, ept=ept, want_alive=True)
+    b = BernoulliBatch(specs, precision=precision, seed=1, block=block, ept=ept, want_alive=True,
+                       occupancy=occupancy)
     s = torch.cuda.Stream()
     b.capture(s)
     b.replay(s)
@@ -56,18 +59,19 @@ def time_shape(specs, precision, block, ept, reps=2) -> float:
 
 
 def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
-                   use_cache: bool = True) -> Tuple[int, int]:
+                   use_cache: bool = True) -> Tuple[int, int, int]:
+    """(block, ept, occupancy) of the fastest candidate for this batch shape."""
     key = _bucket(specs, precision)
     cache = _load() if use_cache else {}
-    if key in cache:
+    if key in cache and len(cache[key]["best"]) == 3:
         return tuple(cache[key]["best"])
     sample = list(specs[::32]) or list(specs)
     times = {}
-    for blk, ept in CANDIDATES[precision]:
-        times[(blk, ept)] = time_shape(sample, precision, blk, ept)
+    for blk, ept, occ in CANDIDATES[precision]:
+        times[(blk, ept, occ)] = time_shape(sample, precision, blk, ept, occ)
     best = min(times, key=times.get)
     cache = _load()
-    cache[key] = {"best": list(best), "ms": {f"{b}x{e}": t for (b, e), t in times.items()}}
+    cache[key] = {"best": list(best), "ms": {f"{b}x{e}/{o}": t for (b, e, o), t in times.items()}}
     try:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
         with open(CACHE, "w") as f:

@@ -105,9 +105,13 @@ class BernoulliBatch:
     def __init__(self, specs: Optional[Sequence[SetSpec]], *, precision: str = "fp32",
                  rng: str = "philox", seed: int = 0, block: int = 256, ept: int = 4,
                  grid: int = 0, want_alive: bool = True, want_fates: bool = False,
-                 uniforms: Optional[np.ndarray] = None, device: str = "cuda", packed=None):
+                 uniforms: Optional[np.ndarray] = None, device: str = "cuda", packed=None,
+                 occupancy: int = 0):
         """``specs`` (a list of SetSpec) or ``packed`` = (sets, segs, bin_offsets,
-        slot_offsets, u_offsets) host arrays as returned by ``pack_host``."""
+        slot_offsets, u_offsets) host arrays as returned by ``pack_host``.
+        ``occupancy`` picks a register-capped FP32 build by the resident CTAs
+        per SM it targets (ept 2: 4 at block 256, 8 at block 128; ept 4: 3 at
+        block 256, 6 at block 128); 0 is the default build."""
         torch = _torch()
         self.lib = _lib.load()
         self.specs = list(specs) if specs is not None else None
@@ -118,6 +122,7 @@ class BernoulliBatch:
         if self.precision == _lib.MCL_FP64 and ept not in (1, 2):
             ept = 2
         self.block, self.ept, self.grid = int(block), int(ept), int(grid)
+        self.occupancy = int(occupancy) if self.precision == _lib.MCL_FP32 else 0
         sets, segs, b_off, s_off, u_off = packed if packed is not None else pack_host(self.specs)
         self.bin_offsets, self.slot_offsets, self.u_offsets = b_off, s_off, u_off
         self.n_bins_total = int(b_off[-1])
@@ -173,6 +178,7 @@ class BernoulliBatch:
         a.n_sets, a.n_segs, a.n_items = len(self.host_sets), len(self.host_segs), self.n_items
         a.slots_per_item, a.max_bins = self.block * self.ept, self.max_bins
         a.precision, a.rng, a.block, a.ept, a.grid = self.precision, self.rng, self.block, self.ept, self.grid
+        a.occupancy = self.occupancy
         a.zero_outputs = zero_outputs
         return a
 

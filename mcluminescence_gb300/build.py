@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = _sources()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 8, len(srcs)))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s, extra_flags, verbose), srcs))
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs

@@ -41,603 +41,20 @@
 #include <algorithm>
 #include <cstdio>
 
-#include "common.cuh"
+#include "kinetics_b_device.cuh"
 
 namespace mcl {
 namespace {
 
-constexpr int kChunk = 256;       // steps per shared-memory chunk of (c_j, q_j)
-constexpr int kHeaderBytes = 256;  // workspace header (ticket)
-
-struct Header {
-  int32_t ticket;
-};
-
-// Kernel parameters: the public launch arguments plus the Philox key
-// schedule k + r*W (r = 0..9), which lands in the constant parameter bank.
-struct KParams {
-  mcl_b_args a;
-  uint32_t ks0[10];
-  uint32_t ks1[10];
-};
-
-// Philox4x32-10 with a precomputed key schedule.
-__device__ __forceinline__ uint4 philox_ks(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                           const KParams& p) {
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint64_t p0 = (uint64_t)kPhiloxM0 * c0;
-    const uint64_t p1 = (uint64_t)kPhiloxM1 * c2;
-    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ p.ks0[r];
-    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ p.ks1[r];
-    c1 = (uint32_t)p1;
-    c3 = (uint32_t)p0;
-    c0 = n0;
-    c2 = n2;
-  }
-  return make_uint4(c0, c1, c2, c3);
-}
-
-// c_j and q_j of local step j of segment sg (FP64 without contraction, in the
-// oracle's evaluation order).
-__device__ __forceinline__ void step_constants(const mcl_set& st, const mcl_segment& sg, int j,
-                                               double& c, double& q) {
-  double dtj, t;
-  if (sg.dt_growth == 1.0) {
-    dtj = sg.dt;
-    t = __dmul_rn(sg.dt, (double)j);
-  } else {
-    const double gj = pow(sg.dt_growth, (double)j);
-    dtj = __dmul_rn(sg.dt, gj);
-    t = __ddiv_rn(__dmul_rn(sg.dt, __dadd_rn(gj, -1.0)), __dadd_rn(sg.dt_growth, -1.0));
-  }
-  const double T = __dadd_rn(sg.T0, __dmul_rn(sg.beta, t));
-  double A = sg.rate_const;
-  if (sg.flags & MCL_SEG_THERMAL) {
-    A = __dadd_rn(A, __dmul_rn(st.s, exp(__ddiv_rn(-st.E, __dmul_rn(st.k_b, T)))));
-  }
-  c = __dmul_rn(dtj, A);
-  q = sg.fill_rate > 0.0 ? -expm1(__dmul_rn(-dtj, sg.fill_rate)) : 0.0;
-}
-
-// Pre-pass: one CTA per set fills its rows of the (c_j, q_j) table.
-template <typename T>
-__global__ void __launch_bounds__(256) kb_tables(const mcl_b_args a) {
-  const int s = blockIdx.x;
-  if (s >= a.n_sets) return;
-  const mcl_set st = a.sets[s];
-  T* tab = reinterpret_cast<T*>(reinterpret_cast<char*>(a.workspace) + kHeaderBytes) + 2 * st.step_offset;
-  int64_t base = 0;
-  for (int g = 0; g < st.seg_count; ++g) {
-    const mcl_segment sg = a.segs[st.seg_begin + g];
-    for (int j = threadIdx.x; j < sg.n_steps; j += blockDim.x) {
-      double c, q;
-      step_constants(st, sg, j, c, q);
-      tab[2 * (base + j)] = (T)c;
-      tab[2 * (base + j) + 1] = (T)q;
-    }
-    base += sg.n_steps;
-  }
-}
-
-__device__ __forceinline__ float r_prime_f(float u) { return cbrtf(-log1pf(-u)); }
-__device__ __forceinline__ double r_prime_d(double u) { return cbrt(-log1p(-u)); }
-
-// Exact FP32-mode tests, kept out of line: they run on ~2e-5 of the trials.
-// The 32-bit uniform of a trial is (h << 16) | lo16: h is the 16-bit field the
-// fast test used, lo16 the low half of word 0 of philox(step, slot, set,
-// TAG_LO), drawn only here.
-__device__ __noinline__ uint32_t full_u32(uint32_t h, uint32_t kstep, uint32_t slot, uint32_t set_id,
-                                          const KParams& P) {
-  const uint4 r = philox_ks(kstep, slot, set_id, kTagLow, P);
-  return (h << 16) | (r.x & 0xffffu);
-}
-
-__device__ __noinline__ bool escape_exact(uint32_t u32, float c, float w) {
-  const float p = -expm1f(-__fmul_rn(c, w));
-  return p >= 1.0f || u32 < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
-}
-
-__device__ __noinline__ bool threshold_exact(uint32_t u32, float q) {
-  return q >= 1.0f || u32 < __float2uint_ru(__fmul_rn(q, 4294967296.0f));
-}
-
-__device__ __noinline__ float refill_w(uint32_t word, float alpha) {
-  const float u = (float)(word >> 8) * 0x1p-24f;
-  return expf(-alpha * r_prime_f(u));
-}
-
-// Sum `v` over the warp and add it to *dst from lane 0 (skipped if all zero).
-__device__ __forceinline__ void warp_flush(uint32_t v, uint32_t* dst) {
-  if (__any_sync(0xffffffffu, v != 0)) {
-    const uint32_t tot = __reduce_add_sync(0xffffffffu, v);
-    if ((threadIdx.x & 31) == 0) atomicAdd(dst, tot);
-  }
-}
-
-template <int BLOCK>
-__device__ __forceinline__ void zero_bins(uint32_t* s_lum, uint32_t* s_alive, int n_bins) {
-  for (int b = threadIdx.x; b < n_bins; b += BLOCK) {
-    s_lum[b] = 0;
-    if (s_alive) s_alive[b] = 0;
-  }
-}
-
-template <int BLOCK>
-__device__ __forceinline__ void flush_bins(const mcl_b_args& a, const mcl_set& st,
-                                           const uint32_t* s_lum, const uint32_t* s_alive) {
-  for (int b = threadIdx.x; b < st.n_bins; b += BLOCK) {
-    const uint32_t v = s_lum[b];
-    if (v) atomicAdd(&a.lum[st.bin_offset + b], v);
-    if (s_alive) {
-      const uint32_t al = s_alive[b];
-      if (al) atomicAdd(&a.alive[st.bin_offset + b], al);
-    }
-  }
-}
-
-__device__ __forceinline__ uint32_t word_of(const uint4& r, int q) {
-  return q == 0 ? r.x : (q == 1 ? r.y : (q == 2 ? r.z : r.w));
-}
-
-// Step t (0..7) of a Philox block uses the 16-bit field h of word t&3: the
-// word's upper half for t < 4, its lower half for t >= 4.  field_f returns the
-// float 2^23 + h with one byte permute (h becomes the low mantissa bits under
-// the exponent of 2^23).
-template <int T>
-__device__ __forceinline__ float field_f(uint32_t word) {
-  return __uint_as_float(__byte_perm(word, 0x4B000000u, (T < 4) ? 0x7432 : 0x7410));
-}
-
-template <int T>
-__device__ __forceinline__ uint32_t field16(uint32_t word) {
-  return (T < 4) ? (word >> 16) : (word & 0xffffu);
-}
-
-// Fast test of the FP32 mode.  The shared-memory step table holds
-// c16 = c * 2^16 and q16 = q * 2^16 (exact power-of-two scalings).  For a
-// filled trap d = fl(2^23 + h - c16 w) (one FFMA), for an empty trap of a
-// filling segment d = fl(2^23 + h - q16).  An event needs u32 < ceil(p 2^32)
-// with u32 = h 2^16 + lo16, hence h < p 2^16 <= c16 w (1 + 2^-21) < c16 w + 2^-5
-// when c w < 1, so the exact value of d is below 2^23 + 2^-5 and d rounds to
-// at most 2^23; d >= kCand = 2^23 + 1 therefore proves that nothing happens.
-// (For c w >= 1, d <= 2^23 + 65535 - 65536 and the trial is always a
-// candidate.)  The test admits h <= c16 w + 1/2, i.e. about c w + 2^-16 of the
-// trials, which go to the exact test.
-constexpr float kCand = 8388609.0f;  // 2^23 + 1
-constexpr float kInv16 = 0x1p-16f;
-
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-  float d;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-  return d;
-}
-
-template <int N>
-__device__ __forceinline__ float min_all(const float (&d)[N]) {
-  float m = d[0];
-  int i = 1;
-#pragma unroll
-  for (; i + 1 < N; i += 2) m = min3f(m, d[i], d[i + 1]);
-  if (i < N) m = fminf(m, d[i]);
-  return m;
-}
-
-// Per-thread state of the FP32 kernel for one work item.
-template <int EPT>
-struct SlotState {
-  float w[EPT];        // w of a filled trap, 0 for an empty one
-  uint32_t slot[EPT];  // slot index within the set
-  uint32_t filled;     // bit i: slot i holds an electron
-};
-
-// Exact test of slot i at step T of the block for a trap that is filled.
-template <int EPT, int T>
-__device__ __forceinline__ bool try_escape(const KParams& P, const mcl_set& st, SlotState<EPT>& S, int i,
-                                           uint32_t word, float c16, int64_t kstep, uint32_t* s_lum, int bin) {
-  const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
-  if (!escape_exact(u32, c16 * kInv16, S.w[i])) return false;
-  S.filled &= ~(1u << i);
-  S.w[i] = 0.0f;
-  atomicAdd(&s_lum[bin], 1u);
-  if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)kstep;
-  return true;
-}
-
-// One step of a filling segment (index T within its Philox block) for all
-// EPT slots: filled traps may escape, empty ones may be refilled.
-template <int EPT, int T>
-__device__ __forceinline__ void step_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                          const uint4 (&r)[EPT], float c16, float q16, int64_t kstep,
-                                          uint32_t* s_lum, int bin, float alpha) {
-  float d[EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const float f = field_f<T>(word_of(r[i], T & 3));
-    d[i] = ((S.filled >> i) & 1u) ? __fmaf_rn(-c16, S.w[i], f) : __fsub_rn(f, q16);
-  }
-  if (min_all<EPT>(d) < kCand) {
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      if (d[i] < kCand) {
-        const uint32_t word = word_of(r[i], T & 3);
-        if ((S.filled >> i) & 1u) {
-          try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin);
-        } else if (S.slot[i] < (uint32_t)st.n_slots) {
-          const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
-          if (threshold_exact(u32, q16 * kInv16)) {
-            const uint4 rr = philox_ks((uint32_t)kstep, S.slot[i], st.set_id, kTagRefill, P);
-            S.w[i] = refill_w(rr.x, alpha);
-            S.filled |= 1u << i;
-          }
-        }
-      }
-    }
-  }
-}
-
-// The steps of one Philox block of a filling segment (8 steps; fewer at the
-// segment's end when FULL is false), one branch per step.
-template <int EPT, bool FULL>
-__device__ __forceinline__ void block_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                           uint32_t blk, const float* s_c, const float* s_q, int jq,
-                                           int nq, int64_t kstep, uint32_t* s_lum, uint32_t* s_alive,
-                                           int& bin, int& to_flush, int spb, int remaining_after,
-                                           float alpha) {
-  uint4 r[EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-#define MCL_STEP(T)                                                                             \
-  if (FULL || (T) < nq) {                                                                       \
-    step_fill<EPT, T>(P, st, S, r, s_c[jq + (T)], s_q[jq + (T)], kstep + (T), s_lum, bin, alpha); \
-    if (--to_flush == 0) {                                                                      \
-      if (s_alive) warp_flush((uint32_t)__popc(S.filled), &s_alive[bin]);                       \
-      ++bin;                                                                                    \
-      to_flush = min(spb, remaining_after - (T));                                               \
-    }                                                                                           \
-  }
-  MCL_STEP(0) MCL_STEP(1) MCL_STEP(2) MCL_STEP(3) MCL_STEP(4) MCL_STEP(5) MCL_STEP(6) MCL_STEP(7)
-#undef MCL_STEP
-}
-
-// Escape candidates of step T of a non-filling block (entered only when the
-// step's minimum d is below kCand).  dcount gains 1 << 4T per escape.
-template <int EPT, int T>
-__device__ __forceinline__ void escapes_of_step(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                                const uint4 (&r)[EPT], float c16, int64_t kstep,
-                                                uint32_t* s_lum, int bin, uint32_t& dcount) {
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    uint32_t word = word_of(r[i], T & 3);
-    // Recompute d here rather than keep the fast pass's 8 x EPT values live.
-    asm volatile("" : "+r"(word));
-    if (((S.filled >> i) & 1u) && __fmaf_rn(-c16, S.w[i], field_f<T>(word)) < kCand) {
-      if (try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin)) dcount += 1u << (4 * T);
-    }
-  }
-}
-
-// The steps of one Philox block of a segment without filling.  Traps only
-// empty here, so a d computed before an escape earlier in the block can only
-// over-report candidates: the fast pass evaluates d for all 8 steps, keeps
-// each step's minimum, and one branch per block enters the exact tests.  The
-// bin bookkeeping runs afterwards for the whole block: alive counts at bin
-// ends inside the block subtract the escapes up to that step, which dcount
-// holds as 4-bit counts per step (prefix sums by one multiply; EPT <= 8
-// keeps every nibble below 16).
-template <int EPT, bool FULL>
-__device__ __forceinline__ void block_nofill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                             uint32_t blk, const float* s_c, int jq, int nq, int64_t kstep,
-                                             uint32_t* s_lum, uint32_t* s_alive, int& bin, int& to_flush,
-                                             int spb, int seg_left) {
-  static_assert(EPT <= 8, "per-step escape counts are 4-bit fields");
-  uint4 r[EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-  const float4 ca = *reinterpret_cast<const float4*>(s_c + jq);
-  const float4 cb = *reinterpret_cast<const float4*>(s_c + jq + 4);
-  const float c16[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
-  float m[8];
-#define MCL_MIN(T)                                                              \
-  if (FULL || (T) < nq) {                                                       \
-    float d[EPT];                                                               \
-    _Pragma("unroll") for (int i = 0; i < EPT; ++i)                             \
-        d[i] = __fmaf_rn(-c16[T], S.w[i], field_f<T>(word_of(r[i], (T) & 3)));  \
-    m[T] = min_all<EPT>(d);                                                     \
-  } else {                                                                      \
-    m[T] = kCand;                                                               \
-  }
-  MCL_MIN(0) MCL_MIN(1) MCL_MIN(2) MCL_MIN(3) MCL_MIN(4) MCL_MIN(5) MCL_MIN(6) MCL_MIN(7)
-#undef MCL_MIN
-  const uint32_t alive0 = (uint32_t)__popc(S.filled);
-  uint32_t dcount = 0;
-  if (min_all<8>(m) < kCand) {
-#define MCL_SLOW(T)                                                                           \
-  if ((FULL || (T) < nq) && m[T] < kCand) {                                                   \
-    int b = bin;                                                                              \
-    for (int tf = to_flush; (T) >= tf; tf += spb) ++b;                                        \
-    escapes_of_step<EPT, T>(P, st, S, r, c16[T], kstep + (T), s_lum, b, dcount);             \
-  }
-    MCL_SLOW(0) MCL_SLOW(1) MCL_SLOW(2) MCL_SLOW(3) MCL_SLOW(4) MCL_SLOW(5) MCL_SLOW(6) MCL_SLOW(7)
-#undef MCL_SLOW
-  }
-  const int n = FULL ? 8 : nq;
-  if (to_flush > n) {
-    to_flush -= n;
-    return;
-  }
-  const uint32_t cum = dcount * 0x11111111u;  // nibble t: escapes in steps 0..t
-  int t = to_flush - 1;                        // block step that ends the current bin
-  for (;;) {
-    if (s_alive) warp_flush(alive0 - ((cum >> (4 * t)) & 0xfu), &s_alive[bin]);
-    ++bin;
-    const int next = min(spb, seg_left - t - 1);
-    if (next == 0) {  // the segment's last step
-      to_flush = 0;
-      return;
-    }
-    if (t + next >= n) {
-      to_flush = t + next - n + 1;
-      return;
-    }
-    t += next;
-  }
-}
-
-// One segment of one work item (FP32).
-template <int BLOCK, int EPT, bool FILL>
-__device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st, const mcl_segment& sg,
-                                            SlotState<EPT>& S, const float2* tab, float* s_c, float* s_q,
-                                            uint32_t* s_lum, uint32_t* s_alive, uint32_t bbase,
-                                            int64_t kglob, float alpha) {
-  const int spb = sg.steps_per_bin;
-  int bin = sg.bin_offset;
-  int to_flush = min(spb, sg.n_steps);
-  for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
-    const int nj = min(kChunk, sg.n_steps - j0);
-    __syncthreads();
-    for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
-      const float2 cq = tab[j0 + jj];
-      s_c[jj] = __fmul_rn(cq.x, 65536.0f);
-      s_q[jj] = __fmul_rn(cq.y, 65536.0f);
-    }
-    __syncthreads();
-    int jq = 0;
-    for (; jq + 8 <= nj; jq += 8) {
-      const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
-      if (FILL)
-        block_fill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush,
-                              spb, sg.n_steps - (j0 + jq) - 1, alpha);
-      else
-        block_nofill<EPT, true>(P, st, S, blk, s_c, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
-                                sg.n_steps - (j0 + jq));
-    }
-    if (jq < nj) {  // the segment's last, partial Philox block
-      const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
-      if (FILL)
-        block_fill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
-                               to_flush, spb, sg.n_steps - (j0 + jq) - 1, alpha);
-      else
-        block_nofill<EPT, false>(P, st, S, blk, s_c, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
-                                 to_flush, spb, sg.n_steps - (j0 + jq));
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// FP32 / Philox kernel
-// ---------------------------------------------------------------------------
-template <int BLOCK, int EPT>
-__global__ void __launch_bounds__(BLOCK) kb_f32(const KParams P) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const mcl_b_args& a = P.a;
-  float* s_c = reinterpret_cast<float*>(smem);
-  float* s_q = s_c + kChunk;
-  uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
-  uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
-  __shared__ int s_item;
-
-  Header* hdr = reinterpret_cast<Header*>(a.workspace);
-  const float2* table = reinterpret_cast<const float2*>(reinterpret_cast<const char*>(a.workspace) + kHeaderBytes);
-  const int tid = threadIdx.x;
-
-  for (;;) {
-    if (tid == 0) s_item = atomicAdd(&hdr->ticket, 1);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= a.n_items) break;
-    const mcl_item item = a.items[it];
-    const mcl_set st = a.sets[item.set];
-    if (st.n_bins > a.max_bins) {  // host validation makes this unreachable
-      report(a.status, MCL_ECAPACITY);
-      __syncthreads();
-      continue;
-    }
-    zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
-
-    const float alpha = (float)st.alpha;
-    SlotState<EPT> S;
-    S.filled = 0;
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int e = item.slot_begin + i * BLOCK + tid;
-      S.slot[i] = (uint32_t)e;
-      S.w[i] = 0.0f;
-      if (e < st.n_filled) {
-        const uint4 r0 = philox_ks(0u, (uint32_t)e, st.set_id, kTagInit, P);
-        S.w[i] = refill_w(r0.x, alpha);
-        S.filled |= 1u << i;
-      }
-    }
-
-    int64_t kglob = 0;  // global step of the set (fates, refill counters)
-    uint32_t bbase = 0;  // Philox blocks used by earlier segments
-    const float2* tab = table + st.step_offset;
-    for (int g = 0; g < st.seg_count; ++g) {
-      const mcl_segment sg = a.segs[st.seg_begin + g];
-      if (sg.fill_rate > 0.0)
-        segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
-      else
-        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
-      bbase += (uint32_t)((sg.n_steps + 7) >> 3);
-      kglob += sg.n_steps;
-    }
-    __syncthreads();
-    flush_bins<BLOCK>(a, st, s_lum, s_alive);
-    __syncthreads();
-  }
-}
-
-// ---------------------------------------------------------------------------
-// FP64 kernel (Philox or injected uniforms): the oracle-parity mode
-// ---------------------------------------------------------------------------
-template <int BLOCK, int EPT, bool INJ>
-__global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const mcl_b_args& a = P.a;
-  double* s_c = reinterpret_cast<double*>(smem);
-  double* s_q = s_c + kChunk;
-  uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
-  uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
-  __shared__ int s_item;
-
-  Header* hdr = reinterpret_cast<Header*>(a.workspace);
-  const double2* table = reinterpret_cast<const double2*>(reinterpret_cast<const char*>(a.workspace) + kHeaderBytes);
-  const int tid = threadIdx.x;
-
-  for (;;) {
-    if (tid == 0) s_item = atomicAdd(&hdr->ticket, 1);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= a.n_items) break;
-    const mcl_item item = a.items[it];
-    const mcl_set st = a.sets[item.set];
-    if (st.n_bins > a.max_bins) {
-      report(a.status, MCL_ECAPACITY);
-      __syncthreads();
-      continue;
-    }
-    zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
-
-    double w[EPT];
-    uint32_t slot[EPT];
-    uint32_t filled = 0;
-    const int64_t n = st.n_slots;
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int e = item.slot_begin + i * BLOCK + tid;
-      slot[i] = (uint32_t)e;
-      w[i] = 0.0;
-      if (e < st.n_slots) {
-        double u;
-        if (INJ) {
-          u = a.uniforms[st.u_offset + e];
-        } else {
-          const uint4 r = philox_ks(0u, (uint32_t)e, st.set_id, kTagInit, P);
-          u = u53(r.x, r.y);
-        }
-        w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u)));
-        if (e < st.n_filled) filled |= 1u << i;
-      }
-    }
-
-    int64_t kglob = 0;
-    uint32_t pbase = 0;
-    const double2* tab = table + st.step_offset;
-    for (int g = 0; g < st.seg_count; ++g) {
-      const mcl_segment sg = a.segs[st.seg_begin + g];
-      const bool fill_on = sg.fill_rate > 0.0;
-      const int spb = sg.steps_per_bin;
-      int to_flush = min(spb, sg.n_steps);
-      int bin = sg.bin_offset;
-      for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
-        const int nj = min(kChunk, sg.n_steps - j0);
-        __syncthreads();
-        for (int jj = tid; jj < nj; jj += BLOCK) {
-          const double2 cq = tab[kglob + j0 + jj];
-          s_c[jj] = cq.x;
-          s_q[jj] = cq.y;
-        }
-        __syncthreads();
-        uint4 r[EPT];
-        for (int jj = 0; jj < nj; ++jj) {
-          const int j = j0 + jj;
-          const int64_t k = kglob + j;
-          if (!INJ && (j & 1) == 0) {
-#pragma unroll
-            for (int i = 0; i < EPT; ++i)
-              r[i] = philox_ks(pbase + (uint32_t)(j >> 1), slot[i], st.set_id, kTagStep, P);
-          }
-          const double c = s_c[jj];
-          const double qv = s_q[jj];
-#pragma unroll
-          for (int i = 0; i < EPT; ++i) {
-            if (slot[i] >= (uint32_t)st.n_slots) continue;
-            double u;
-            if (INJ) {
-              u = a.uniforms[st.u_offset + n + k * n + slot[i]];
-            } else {
-              u = (j & 1) ? u53(r[i].z, r[i].w) : u53(r[i].x, r[i].y);
-            }
-            if ((filled >> i) & 1u) {
-              const double p = -expm1(__dmul_rn(-c, w[i]));
-              if (u < p) {
-                filled &= ~(1u << i);
-                atomicAdd(&s_lum[bin], 1u);
-                if (a.fates) a.fates[st.slot_offset + slot[i]] = (int32_t)k;
-              }
-            } else if (!INJ && fill_on && u < qv) {
-              const uint4 rr = philox_ks((uint32_t)k, slot[i], st.set_id, kTagRefill, P);
-              w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u53(rr.x, rr.y))));
-              filled |= 1u << i;
-            }
-          }
-          if (--to_flush == 0) {
-            if (s_alive) warp_flush((uint32_t)__popc(filled), &s_alive[bin]);
-            ++bin;
-            to_flush = min(spb, sg.n_steps - j - 1);
-          }
-        }
-      }
-      pbase += (uint32_t)((sg.n_steps + 1) >> 1);
-      kglob += sg.n_steps;
-    }
-    __syncthreads();
-    flush_bins<BLOCK>(a, st, s_lum, s_alive);
-    __syncthreads();
-  }
-}
-
-using KernelFn = void (*)(const KParams);
-
-template <int BLOCK>
-KernelFn pick_f32(int ept) {
-  switch (ept) {
-    case 2: return kb_f32<BLOCK, 2>;
-    case 4: return kb_f32<BLOCK, 4>;
-    case 8: return kb_f32<BLOCK, 8>;
-  }
-  return nullptr;
-}
-
 KernelFn pick_kernel(const mcl_b_args& a) {
   if (a.precision == MCL_FP32) {
     if (a.rng != MCL_RNG_PHILOX) return nullptr;
-    switch (a.block) {
-      case 128: return pick_f32<128>(a.ept);
-      case 256: return pick_f32<256>(a.ept);
-    }
+    const int o = a.occupancy;
+    if (a.block == 128) return a.ept == 2 ? b_f32_128_e2(o) : a.ept == 4 ? b_f32_128_e4(o) : a.ept == 8 ? b_f32_128_e8(o) : nullptr;
+    if (a.block == 256) return a.ept == 2 ? b_f32_256_e2(o) : a.ept == 4 ? b_f32_256_e4(o) : a.ept == 8 ? b_f32_256_e8(o) : nullptr;
     return nullptr;
   }
-  if (a.precision == MCL_FP64 && a.block == 256) {
-    if (a.rng == MCL_RNG_INJECTED) {
-      if (a.ept == 1) return kb_f64<256, 1, true>;
-      if (a.ept == 2) return kb_f64<256, 2, true>;
-    } else {
-      if (a.ept == 1) return kb_f64<256, 1, false>;
-      if (a.ept == 2) return kb_f64<256, 2, false>;
-    }
-  }
+  if (a.precision == MCL_FP64) return b_pick_f64(a.block, a.ept, a.rng == MCL_RNG_INJECTED);
   return nullptr;
 }
 

@@ -1,0 +1,12 @@
+// FP32 Bernoulli kernel, 256 threads per CTA, 8 slots per thread (one
+// translation unit per variant so that the variants compile in parallel).
+// occupancy 0 = the default build.
+#include "kinetics_b_device.cuh"
+
+namespace mcl {
+
+KernelFn b_f32_256_e8(int occupancy) {
+  return occupancy == 0 ? kb_f32<256, 8> : nullptr;
+}
+
+}  // namespace mcl

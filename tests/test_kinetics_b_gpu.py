@@ -82,11 +82,13 @@ def test_fp32_fates_match_fp64_oracle_on_same_stream():
     assert total_mism <= 2
 
 
-@pytest.mark.parametrize("block,ept", [(128, 2), (256, 2), (256, 8), (128, 8)])
-def test_fp32_launch_shape_invariance(block, ept):
+@pytest.mark.parametrize("block,ept,occ", [(128, 2, 0), (256, 2, 0), (256, 8, 0), (128, 8, 0),
+                                            (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)])
+def test_fp32_launch_shape_invariance(block, ept, occ):
     specs = mixed_specs()
     ref = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=256, ept=4)
-    got = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=block, ept=ept)
+    got = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=block, ept=ept,
+                         occupancy=occ)
     assert np.array_equal(ref.lum, got.lum)
     assert np.array_equal(ref.alive, got.alive)
     assert np.array_equal(ref.fates, got.fates)
@@ -187,3 +189,8 @@ def test_fill_fade_irsl_sequence_fp32_fates():
         assert abs(int(res.alive_of(i)[-1]) - int(alive[-1])) <= 2
     assert ev > 100
     assert mism <= 2
+
+
+def test_fp32_unknown_register_capped_build_is_rejected():
+    with pytest.raises(Exception, match="invalid argument|EINVAL|MCL_EINVAL"):
+        simulate_batch(mixed_specs()[:2], precision="fp32", seed=5, block=256, ept=8, occupancy=3)
