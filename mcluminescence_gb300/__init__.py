@@ -22,3 +22,6 @@ __all__ += ["simulate", "run_kinetics", "run_params", "write_table"]
 from .kinetics import TLTrapSim  # noqa: F401,E402
 
 __all__ += ["TLTrapSim"]
+from .shard import run_sharded, shard_for_rank, simulate_batch_sharded  # noqa: F401,E402
+
+__all__ += ["simulate_batch_sharded", "run_sharded", "shard_for_rank"]
