@@ -310,6 +310,33 @@ int mcl_b_graph_create(const mcl_b_args* args, void* stream, void** graph_out);
 int mcl_graph_launch(void* graph, void* stream);
 int mcl_graph_destroy(void* graph);
 
+/* ---- presentation binning and smoothing --------------------------------- */
+/* The glow curves src/class/plots.py:52-74 (plot_TL) draws from simulate()'s
+ * tables x_ax, lum [steps][sims][runs] (device, FP64): per run the steps with
+ * x_ax[:, 0, r] > 0 at T = T_start[r] + T_rate[r] * t, histogrammed into
+ * bin_width-wide bins from 0 (hist_and_smooth, plots.py:39-47).
+ * mcl_glow_extent writes per run the number of bin edges,
+ * ceil((max T + bin_width) / bin_width), or -1 if no step has t > 0 (the
+ * reference raises there).  mcl_glow_hist fills hist (bin_offsets[runs+1]
+ * from those counts: n_edges - 1 bins per run) with the replica-mean event
+ * count per bin divided by bin_width; counts is scratch of n_bins_total
+ * words; *status becomes MCL_EINVAL if a lum entry is not a 0/1 flag. */
+int mcl_glow_extent(const double* x_ax, int32_t steps, int32_t sims, int32_t runs,
+                    const double* T_start, const double* T_rate, double bin_width, int64_t* n_edges,
+                    void* stream);
+int mcl_glow_hist(const double* x_ax, const double* lum, int32_t steps, int32_t sims, int32_t runs,
+                  const double* T_start, const double* T_rate, double bin_width,
+                  const int64_t* bin_offsets, int64_t n_bins_total, uint32_t* counts, double* hist,
+                  int32_t* status, void* stream);
+/* running_mean (plots.py:19-21) of every curve: out = 'valid' boxcar of width
+ * k over in / divisor.  in_type 0 = double, 1 = uint32 (e.g. Bernoulli bins);
+ * curves are [in_offsets[c], in_offsets[c+1]); out_offsets must give
+ * n - k + 1 outputs per curve of n >= k values and k - n + 1 (all equal to
+ * the curve's sum / k) for 0 < n < k; max_out = largest output count. */
+int mcl_running_mean(int32_t in_type, const void* in, const int64_t* in_offsets, int32_t n_curves,
+                     int32_t k, double divisor, const int64_t* out_offsets, int64_t max_out, double* out,
+                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,3 +25,6 @@ __all__ += ["TLTrapSim"]
 from .shard import run_sharded, shard_for_rank, simulate_batch_sharded  # noqa: F401,E402
 
 __all__ += ["simulate_batch_sharded", "run_sharded", "shard_for_rank"]
+from .post import running_mean, smooth_batch, tl_glow_curves, tl_glow_curves_from_configs  # noqa: F401,E402
+
+__all__ += ["tl_glow_curves", "tl_glow_curves_from_configs", "running_mean", "smooth_batch"]
