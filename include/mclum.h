@@ -302,6 +302,20 @@ int mcl_mse_loss(int32_t M, int32_t N, int32_t n_valid, const float* out, int32_
  * W[rows][cols] and Wt[cols][rows] when non-null.  step counts from 1. */
 int mcl_adam(int32_t rows, int32_t cols, float* p, const float* g, float* m1, float* m2, float lr,
              float b1, float b2, float eps, int32_t step, void* W, void* Wt, void* stream);
+/* The same Adam step for up to 16 tensors in one launch (the arrays are
+ * host memory holding device pointers; W / Wt may be NULL). */
+typedef struct mcl_adam_tensor {
+  float* p;
+  const float* g;
+  float* m1;
+  float* m2;
+  void* W;
+  void* Wt;
+  int32_t rows;
+  int32_t cols;
+} mcl_adam_tensor;
+int mcl_adam_multi(const mcl_adam_tensor* tensors, int32_t n, float lr, float b1, float b2, float eps,
+                   int32_t step, void* stream);
 int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream);
 
 /* ---- CUDA graphs -------------------------------------------------------- */

@@ -12,6 +12,7 @@
 // multiples of 128), and gemm_nt with mma.sync m16n8k16 instructions fed by
 // ldmatrix from padded shared memory (64 x 64 x 32 tiles) for other shapes.
 // The host pads 6 -> 64 inputs and 200 -> 256 outputs with zeros.
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -133,33 +134,50 @@ __global__ void __launch_bounds__(128) gemm_nt(int M, int N, int K, const __nv_b
 
 // dZ = dY * gelu'(Z) (or dZ = dY for a linear layer) as bf16 in [M][N] and
 // [N][M], and db[n] += sum over this CTA's rows of dZ (fp32 atomics).
+// dZ = dY * GELU'(Z) (or dY) in bf16, both as dZ[M][N] and dZt[N][M], and
+// the bias gradient db[n] += sum_m dZ.  CTA: 32 rows x 64 columns, 256
+// threads (64 columns x 4 row groups of 8 rows); the transposed copy goes
+// through shared memory so that both stores are row-contiguous, and the
+// column sums meet in shared memory (one atomic per column per CTA).
 __global__ void __launch_bounds__(256) act_backward(int M, int N, const float* __restrict__ dY, int lddy,
                                                     const float* __restrict__ Z, int ldz, int gelu_on,
                                                     __nv_bfloat16* __restrict__ dZ, int lddz,
                                                     __nv_bfloat16* __restrict__ dZt, int lddzt,
                                                     float* __restrict__ db) {
-  // CTA: 32 rows x 256 columns chunk; each thread one column, loops the rows
-  const int n = blockIdx.x * 256 + threadIdx.x;
+  __shared__ __nv_bfloat16 tile[64][34];  // [column][row], padded
+  __shared__ float part[4][64];
+  const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+  const int n0 = blockIdx.x * 64, n = n0 + tx;
   const int m0 = blockIdx.y * 32;
-  if (n >= N) return;
   float colsum = 0.0f;
-  for (int r = 0; r < 32; ++r) {
-    const int m = m0 + r;
-    if (m >= M) break;
-    float d = dY[(size_t)m * lddy + n];
-    if (gelu_on) d *= gelu_grad(Z[(size_t)m * ldz + n]);
-    const __nv_bfloat16 b = __float2bfloat16_rn(d);
-    dZ[(size_t)m * lddz + n] = b;
-    dZt[(size_t)n * lddzt + m] = b;
-    colsum += d;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = ty + 4 * i, m = m0 + r;
+    __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
+    if (m < M && n < N) {
+      float d = dY[(size_t)m * lddy + n];
+      if (gelu_on) d *= gelu_grad(Z[(size_t)m * ldz + n]);
+      b = __float2bfloat16_rn(d);
+      dZ[(size_t)m * lddz + n] = b;
+      colsum += d;
+    }
+    tile[tx][r] = b;
   }
-  atomicAdd(&db[n], colsum);
+  part[ty][tx] = colsum;
+  __syncthreads();
+  if (ty == 0 && n < N) atomicAdd(&db[n], (part[0][tx] + part[1][tx]) + (part[2][tx] + part[3][tx]));
+  for (int e = threadIdx.x; e < 64 * 32; e += 256) {
+    const int c = e >> 5, r = e & 31;  // consecutive threads: consecutive m of one dZt row
+    if (n0 + c < N && m0 + r < M) dZt[(size_t)(n0 + c) * lddzt + m0 + r] = tile[c][r];
+  }
 }
 
-// loss += sum over valid columns of (out - target)^2; dOut = 2 (out - target) * scale
+// loss += sum over valid columns of (out - target)^2; dOut = 2 (out - target) * scale.
+// One atomic per CTA.
 __global__ void __launch_bounds__(256) mse_loss(int M, int N, int n_valid, const float* __restrict__ out, int ldo,
                                                 const float* __restrict__ target, int ldt, float scale,
                                                 float* __restrict__ dout, int ldd, float* __restrict__ loss) {
+  __shared__ float warp_part[8];
   const int64_t total = (int64_t)M * N;
   float part = 0.0f;
   for (int64_t idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * 256) {
@@ -172,7 +190,13 @@ __global__ void __launch_bounds__(256) mse_loss(int M, int N, int n_valid, const
     dout[(size_t)m * ldd + n] = 2.0f * d * scale;
   }
   for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, part);
+  if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < 8; ++w) t += warp_part[w];
+    atomicAdd(loss, t);
+  }
 }
 
 // Adam on fp32 master weights; refreshes the bf16 copies W[rows][cols] and
@@ -195,6 +219,32 @@ __global__ void __launch_bounds__(256) adam_update(int rows, int cols, float* __
     const __nv_bfloat16 q = __float2bfloat16_rn(pi);
     if (W) W[i] = q;
     if (Wt) Wt[(size_t)(i % cols) * rows + i / cols] = q;
+  }
+}
+
+// Adam over up to 16 tensors in one launch (blockIdx.y = tensor).
+struct AdamMulti {
+  mcl_adam_tensor t[16];
+};
+
+__global__ void __launch_bounds__(256) adam_multi(const AdamMulti A, float lr, float b1, float b2, float eps,
+                                                  float bc1, float bc2) {
+  const mcl_adam_tensor& T = A.t[blockIdx.y];
+  const int64_t n = (int64_t)T.rows * T.cols;
+  __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(T.W);
+  __nv_bfloat16* Wt = reinterpret_cast<__nv_bfloat16*>(T.Wt);
+  for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+    const float gi = T.g[i];
+    const float a = b1 * T.m1[i] + (1.0f - b1) * gi;
+    const float b = b2 * T.m2[i] + (1.0f - b2) * gi * gi;
+    T.m1[i] = a;
+    T.m2[i] = b;
+    const float mh = a / bc1, vh = b / bc2;
+    const float pi = T.p[i] - lr * mh / (sqrtf(vh) + eps);
+    T.p[i] = pi;
+    const __nv_bfloat16 q = __float2bfloat16_rn(pi);
+    if (W) W[i] = q;
+    if (Wt) Wt[(size_t)(i % T.cols) * T.rows + i / T.cols] = q;
   }
 }
 
@@ -289,83 +339,165 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Copy rows [r0, r0 + rows) x K slab [k0, k0 + 64) of a k-contiguous bf16
-// matrix into the core-matrix layout.
-__device__ __forceinline__ void stage(unsigned char* dst, const __nv_bfloat16* src, int ld, int r0, int rows,
-                                      int k0) {
-  for (int c = threadIdx.x; c < rows * (kKS / 8); c += blockDim.x) {
-    const int r = c / (kKS / 8), kc = c % (kKS / 8);
-    const uint4 v = *reinterpret_cast<const uint4*>(&src[(size_t)(r0 + r) * ld + k0 + kc * 8]);
-    *reinterpret_cast<uint4*>(dst + ((r >> 3) * (kKS / 8) + kc) * 128 + (r & 7) * 16) = v;
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Start copying rows [m0, m0 + 128) of A and [n0, n0 + NT) of B (k-contiguous
+// bf16) x K slab [k0, k0 + 64) into the core-matrix layout at shared
+// addresses dA / dB (16-byte asynchronous copies; no registers held).
+template <int NT>
+__device__ __forceinline__ void issue_slab(uint32_t dA, uint32_t dB, const __nv_bfloat16* A, int lda,
+                                           const __nv_bfloat16* B, int ldb, int m0, int n0, int k0) {
+  constexpr int PA = kM * (kKS / 8) / 128, PB = NT * (kKS / 8) / 128;
+#pragma unroll
+  for (int i = 0; i < PA; ++i) {
+    const int c = threadIdx.x + 128 * i, r = c / (kKS / 8), kc = c % (kKS / 8);
+    cp_async16(dA + ((r >> 3) * (kKS / 8) + kc) * 128 + (r & 7) * 16, &A[(size_t)(m0 + r) * lda + k0 + kc * 8]);
+  }
+#pragma unroll
+  for (int i = 0; i < PB; ++i) {
+    const int c = threadIdx.x + 128 * i, r = c / (kKS / 8), kc = c % (kKS / 8);
+    cp_async16(dB + ((r >> 3) * (kKS / 8) + kc) * 128 + (r & 7) * 16, &B[(size_t)(n0 + r) * ldb + k0 + kc * 8]);
   }
 }
 
+constexpr int kStageA = kM * kKS * 2;  // bytes of one staged A slab
+constexpr int kStages = 3;             // slabs in flight: two loading while one multiplies
+
+// Dynamic shared memory: kStages A and B slabs for the main loop, reused by
+// the epilogue for the fp32 tile [128][NT+1] and the bf16 tile [128][NT+2].
+template <int NT>
+constexpr int smem_bytes() {
+  return kStages * (kStageA + NT * kKS * 2) > 128 * (NT + 1) * 4 + 128 * (NT + 2) * 2
+             ? kStages * (kStageA + NT * kKS * 2)
+             : 128 * (NT + 1) * 4 + 128 * (NT + 2) * 2;
+}
+
+// Split-K: gridDim.z CTAs, launched as one thread-block cluster along z, each
+// accumulate a K/gridDim.z range of the same tile; the partial tiles meet in
+// distributed shared memory and every CTA sums 128/gridDim.z of the rows over
+// the cluster in rank order (deterministic).  Only the plain fp32 epilogue
+// uses it (the weight gradients, whose K is the batch).
 template <int EPI, int NT>
 __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
                                                   const __nv_bfloat16* __restrict__ B, int ldb,
                                                   const float* __restrict__ bias, float* __restrict__ C, int ldc,
                                                   __nv_bfloat16* __restrict__ Y, int ldy,
                                                   __nv_bfloat16* __restrict__ Yt, int ldyt, int32_t* err) {
-  __shared__ __align__(1024) unsigned char sA[kM * kKS * 2];
-  __shared__ __align__(1024) unsigned char sB[NT * kKS * 2];
-  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar[kStages];
   __shared__ uint32_t tmem_slot;
+  // slab buffer q: A at smem + q * kStageA, B at smem + kStages * kStageA + q * NT * kKS * 2
+  const uint32_t sbase = smem_u32(smem);
+  auto slabA = [&](int q) { return sbase + q * kStageA; };
+  auto slabB = [&](int q) { return sbase + kStages * kStageA + q * NT * kKS * 2; };
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * kM, n0 = blockIdx.x * NT;
-  const uint32_t mbar_a = smem_u32(&mbar);
+  const int splits = gridDim.z;
+  const int kper = K / splits, kbeg = blockIdx.z * kper, nk = kper / kKS;
+  const uint32_t mb0 = smem_u32(&mbar[0]);  // barrier q at mb0 + 8 q; MMA j commits to barrier j % 3
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), NT);
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+    for (int q = 0; q < kStages; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0 + 8 * q) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // prologue: slabs 0 and 1 in flight (one commit group per slab, empty if absent)
+  issue_slab<NT>(slabA(0), slabB(0), A, lda, B, ldb, m0, n0, kbeg);
+  cp_async_commit();
+  if (nk > 1) issue_slab<NT>(slabA(1), slabB(1), A, lda, B, ldb, m0, n0, kbeg + kKS);
+  cp_async_commit();
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_slot;
   constexpr uint32_t idesc = idesc_bf16(kM, NT);
-  uint32_t phase = 0;
   bool ok = true;
-  for (int k0 = 0; k0 < K; k0 += kKS) {
-    stage(sA, A, lda, m0, kM, k0);
-    stage(sB, B, ldb, n0, NT, k0);
+  for (int it = 0; it < nk; ++it) {
+    const int q = it % kStages;
+    cp_async_wait_1();  // this thread's copies of slab it have landed
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;  // everyone's copies visible; all agree on ok
+    if (!ok) break;
     if (tid == 0) {
       fence_after();
 #pragma unroll
       for (int kk = 0; kk < kKS / 16; ++kk) {
-        const uint64_t ad = sdesc(smem_u32(sA) + kk * 256, 128, 1024);
-        const uint64_t bd = sdesc(smem_u32(sB) + kk * 256, 128, 1024);
-        mma(tmem, ad, bd, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
+        const uint64_t ad = sdesc(slabA(q) + kk * 256, 128, 1024);
+        const uint64_t bd = sdesc(slabB(q) + kk * 256, 128, 1024);
+        mma(tmem, ad, bd, idesc, (it > 0 || kk > 0) ? 1u : 0u);
       }
-      commit(mbar_a);
+      commit(mb0 + 8 * q);
     }
     __syncwarp();
-    const bool got = mbar_wait(mbar_a, phase);
-    ok = __syncthreads_and(got ? 1 : 0) != 0;   // every thread leaves the loop together
-    phase ^= 1;
-    fence_after();
-    if (!ok) break;
+    if (it + 2 < nk) {
+      // slab it + 2 reuses the buffer of slab it - 1: wait for that MMA first
+      if (it >= 1) {
+        const int j = it - 1;
+        if (!mbar_wait(mb0 + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u)) ok = false;
+        fence_after();
+      }
+      if (ok) issue_slab<NT>(slabA((it + 2) % kStages), slabB((it + 2) % kStages), A, lda, B, ldb, m0, n0,
+                             kbeg + (it + 2) * kKS);
+    }
+    cp_async_commit();
   }
-  if (!ok) {
-    if (tid == 0) atomicExch(err, 1);
-  } else {
-    const int m = m0 + 32 * warp + lane;
+  if (ok) {  // the last commit covers every MMA before it
+    const int j = nk - 1;
+    if (!mbar_wait(mb0 + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u)) ok = false;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  fence_after();
+  if (!ok && tid == 0) atomicExch(err, 1);
+
+  // Accumulator -> fp32 tile in shared memory (thread = row, as tcgen05.ld
+  // delivers it), then stores in row order (coalesced).
+  constexpr int FS = NT + 1, HS = NT + 2;
+  float* ftile = reinterpret_cast<float*>(smem);
+  const int row = 32 * warp + lane;
+  if (ok) {
 #pragma unroll 1
     for (int c0 = 0; c0 < NT; c0 += 16) {
       float v[16];
       ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int n = n0 + c0 + j;
-        float x = v[j];
-        if (EPI != EPI_F32) x += bias[n];
-        C[(size_t)m * ldc + n] = x;
-        if (EPI == EPI_BIAS_GELU) {
-          const __nv_bfloat16 y = __float2bfloat16_rn(gelu(x));
-          Y[(size_t)m * ldy + n] = y;
-          if (Yt) Yt[(size_t)n * ldyt + m] = y;
-        }
+      for (int j = 0; j < 16; ++j) ftile[row * FS + c0 + j] = v[j];
+    }
+  }
+  if (splits > 1) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    cluster.sync();  // every partial tile is in its CTA's shared memory
+    const int rows = kM / splits, r0 = (int)cluster.block_rank() * rows;
+    for (int e = tid; e < rows * NT; e += blockDim.x) {
+      const int r = r0 + e / NT, c = e % NT;
+      float acc = 0.0f;
+      for (int q = 0; q < splits; ++q) acc += cluster.map_shared_rank(ftile, q)[r * FS + c];
+      if (ok) C[(size_t)(m0 + r) * ldc + n0 + c] = acc;
+    }
+    cluster.sync();  // no CTA leaves while another reads its tile
+  } else {
+    __syncthreads();
+    __nv_bfloat16* htile = reinterpret_cast<__nv_bfloat16*>(smem + 128 * FS * 4);
+    for (int e = tid; e < kM * NT; e += blockDim.x) {
+      const int r = e / NT, c = e % NT;
+      float x = ftile[r * FS + c];
+      if (EPI != EPI_F32) x += bias[n0 + c];
+      if (ok) C[(size_t)(m0 + r) * ldc + n0 + c] = x;
+      if (EPI == EPI_BIAS_GELU) {
+        const __nv_bfloat16 y = __float2bfloat16_rn(gelu(x));
+        if (ok) Y[(size_t)(m0 + r) * ldy + n0 + c] = y;
+        htile[r * HS + c] = y;
+      }
+    }
+    if (EPI == EPI_BIAS_GELU && Yt) {
+      __syncthreads();
+      for (int e = tid; e < kM * NT; e += blockDim.x) {
+        const int c = e / kM, r = e % kM;  // consecutive threads: consecutive m of Yt[n][m]
+        if (ok) Yt[(size_t)(n0 + c) * ldyt + m0 + r] = htile[r * HS + c];
       }
     }
   }
@@ -411,7 +543,7 @@ extern "C" int mcl_act_backward(int32_t M, int32_t N, const float* dY, int32_t l
                                 int32_t gelu_on, void* dZ, int32_t lddz, void* dZt, int32_t lddzt, float* db,
                                 void* stream) {
   if (M <= 0 || N <= 0 || !dY || !dZ || !dZt || !db || (gelu_on && !Z)) return MCL_EINVAL;
-  dim3 grid((N + 255) / 256, (M + 31) / 32);
+  dim3 grid((N + 63) / 64, (M + 31) / 32);
   act_backward<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
       M, N, dY, lddy, Z, ldz, gelu_on, reinterpret_cast<__nv_bfloat16*>(dZ), lddz,
       reinterpret_cast<__nv_bfloat16*>(dZt), lddzt, db);
@@ -424,7 +556,7 @@ extern "C" int mcl_mse_loss(int32_t M, int32_t N, int32_t n_valid, const float* 
                             float* loss, void* stream) {
   if (M <= 0 || N <= 0 || n_valid > N || !out || !target || !dout || !loss) return MCL_EINVAL;
   const int64_t total = (int64_t)M * N;
-  const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 608);
   mse_loss<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(M, N, n_valid, out, ldo, target, ldt,
                                                                       scale, dout, ldd, loss);
   MCL_CUDA_TRY(cudaGetLastError());
@@ -444,6 +576,24 @@ extern "C" int mcl_adam(int32_t rows, int32_t cols, float* p, const float* g, fl
   return MCL_OK;
 }
 
+extern "C" int mcl_adam_multi(const mcl_adam_tensor* tensors, int32_t n, float lr, float b1, float b2, float eps,
+                              int32_t step, void* stream) {
+  if (!tensors || n < 1 || n > 16 || step < 1) return MCL_EINVAL;
+  AdamMulti A;
+  int64_t most = 0;
+  for (int i = 0; i < n; ++i) {
+    const mcl_adam_tensor& t = tensors[i];
+    if (t.rows <= 0 || t.cols <= 0 || !t.p || !t.g || !t.m1 || !t.m2) return MCL_EINVAL;
+    A.t[i] = t;
+    most = std::max<int64_t>(most, (int64_t)t.rows * t.cols);
+  }
+  const float bc1 = 1.0f - powf(b1, (float)step), bc2 = 1.0f - powf(b2, (float)step);
+  dim3 grid((unsigned)std::min<int64_t>((most + 255) / 256, 256), (unsigned)n);
+  adam_multi<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A, lr, b1, b2, eps, bc1, bc2);
+  MCL_CUDA_TRY(cudaGetLastError());
+  return MCL_OK;
+}
+
 extern "C" int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream) {
   if (n < 0 || (n > 0 && (!x || !y))) return MCL_EINVAL;
   if (n == 0) return MCL_OK;
@@ -452,6 +602,39 @@ extern "C" int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream)
   MCL_CUDA_TRY(cudaGetLastError());
   return MCL_OK;
 }
+
+namespace mcl {
+namespace {
+template <int EPI>
+int launch_tc(dim3 grid, int splits, int M, int N, int K, const __nv_bfloat16* a, int lda, const __nv_bfloat16* b,
+              int ldb, const float* bias, float* C, int ldc, __nv_bfloat16* y, int ldy, __nv_bfloat16* yt,
+              int ldyt, int32_t* err, cudaStream_t s) {
+  constexpr int NT = 64;
+  auto kern = tc::gemm_nt_tc<EPI, NT>;
+  constexpr int smem = tc::smem_bytes<NT>();
+  MCL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  if (splits == 1) {
+    kern<<<grid, 128, smem, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err);
+    MCL_CUDA_TRY(cudaGetLastError());
+    return MCL_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid.x, grid.y, (unsigned)splits);
+  cfg.blockDim = dim3(128, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 1;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = (unsigned)splits;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  MCL_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err));
+  return MCL_OK;
+}
+}  // namespace
+}  // namespace mcl
 
 extern "C" int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                               const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
@@ -463,17 +646,26 @@ extern "C" int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K,
   if (epilogue != EPI_F32 && !bias) return MCL_EINVAL;
   if (epilogue == EPI_BIAS_GELU && (!Y || ldy < N || (Yt && ldyt < M))) return MCL_EINVAL;
   dim3 grid(N / NT, M / tc::kM);
+  // Few output tiles and a long K (weight gradients, K = batch): split K over
+  // a cluster of up to 8 CTAs, at least two 64-wide slabs each.
+  int splits = 1;
+  const int slabs = K / tc::kKS;
+  if (epilogue == EPI_F32 && (int)(grid.x * grid.y) < 64) {
+    for (int sp = 8; sp >= 2; sp >>= 1)
+      if (slabs % sp == 0 && slabs / sp >= 2) {
+        splits = sp;
+        break;
+      }
+  }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const auto* a = reinterpret_cast<const __nv_bfloat16*>(A);
   const auto* b = reinterpret_cast<const __nv_bfloat16*>(B);
   auto* y = reinterpret_cast<__nv_bfloat16*>(Y);
   auto* yt = reinterpret_cast<__nv_bfloat16*>(Yt);
   switch (epilogue) {
-    case EPI_F32: tc::gemm_nt_tc<EPI_F32, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
-    case EPI_BIAS: tc::gemm_nt_tc<EPI_BIAS, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
-    case EPI_BIAS_GELU: tc::gemm_nt_tc<EPI_BIAS_GELU, NT><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err); break;
-    default: return MCL_EINVAL;
+    case EPI_F32: return launch_tc<EPI_F32>(grid, splits, M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err, s);
+    case EPI_BIAS: return launch_tc<EPI_BIAS>(grid, 1, M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err, s);
+    case EPI_BIAS_GELU: return launch_tc<EPI_BIAS_GELU>(grid, 1, M, N, K, a, lda, b, ldb, bias, C, ldc, y, ldy, yt, ldyt, err, s);
   }
-  MCL_CUDA_TRY(cudaGetLastError());
-  return MCL_OK;
+  return MCL_EINVAL;
 }

@@ -4,9 +4,11 @@ A small MLP maps six physics parameters -- trap depth E, log10 s, the
 tunnelling coefficient alpha, log10 rho', log10 dose and log10 heating rate --
 to the 200-bin log glow curve that the Monte Carlo kernel produces (TL ramp
 0 -> 500 degC, 2.5 degC bins, 2,000 traps).  Forward, backward and Adam run in
-the library's own kernels (``mcl_gemm_nt`` with fused bias+GELU epilogue on
-BF16 operands with FP32 accumulation, ``mcl_act_backward``, ``mcl_mse_loss``,
-``mcl_adam``); torch only provides device memory and the stream.
+the library's own kernels (``mcl_gemm_nt_tc``: tcgen05 tensor-core GEMM with
+the accumulator in tensor memory and a fused bias+GELU epilogue, BF16
+operands, FP32 accumulation, split-K over a thread-block cluster for the
+weight gradients; ``mcl_act_backward``, ``mcl_mse_loss``, ``mcl_adam_multi``);
+torch only provides device memory and the stream.
 
 The reference has no surrogate: its optimiser (src/class/optimizer.py:93-111)
 evaluates every differential-evolution candidate with a full simulation.  Here
@@ -222,16 +224,20 @@ class SurrogateMLP:
             dY, lddy = self.dY[l], k
 
     def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        """One Adam step on every weight and bias (one launch)."""
         self.step_count += 1
-        for L in self.layers:
-            n, k = L.W.shape
-            _lib.check(self.lib.mcl_adam(n, k, self._p(L.W), self._p(L.gW), self._p(L.mW), self._p(L.vW),
-                                         C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
-                                         self.step_count, self._p(L.Wb), self._p(L.Wt), self._s()),
-                       "mcl_adam")
-            _lib.check(self.lib.mcl_adam(1, n, self._p(L.b), self._p(L.gb), self._p(L.mb), self._p(L.vb),
-                                         C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
-                                         self.step_count, None, None, self._s()), "mcl_adam")
+        if getattr(self, "_adam_arr", None) is None:
+            ts = []
+            for L in self.layers:
+                n, k = L.W.shape
+                ts.append(_lib.AdamTensor(L.W.data_ptr(), L.gW.data_ptr(), L.mW.data_ptr(), L.vW.data_ptr(),
+                                          L.Wb.data_ptr(), L.Wt.data_ptr(), n, k))
+                ts.append(_lib.AdamTensor(L.b.data_ptr(), L.gb.data_ptr(), L.mb.data_ptr(), L.vb.data_ptr(),
+                                          None, None, 1, n))
+            self._adam_arr = (_lib.AdamTensor * len(ts))(*ts)
+        _lib.check(self.lib.mcl_adam_multi(C.cast(self._adam_arr, C.c_void_p), len(self._adam_arr), C.c_float(lr),
+                                           C.c_float(b1), C.c_float(b2), C.c_float(eps), self.step_count,
+                                           self._s()), "mcl_adam_multi")
 
     def state_dict(self) -> dict:
         """FP32 master weights and biases (host tensors), for checkpoints."""
@@ -300,11 +306,11 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
           n_traps: int = N_TRAPS, use_graph: bool = True) -> List[float]:
     """Adam on random mini-batches; cosine decay from lr to lr_final.
 
-    One step (batch gather, forward, loss, backward, Adam) is ~40 small
-    kernels, so it is captured once in a CUDA graph and replayed; the
-    learning rate and step count reach the graph through device scalars.
-    Returns the loss (mean squared error of the log curve) every log_every
-    steps."""
+    One step (batch gather, forward, loss, backward) is ~25 small kernels,
+    so it is captured once in a CUDA graph and replayed; Adam, whose learning
+    rate and step count are launch arguments, runs after each replay as one
+    multi-tensor launch.  Returns the loss (mean squared error of the log
+    curve) every log_every steps."""
     t = model.torch
     X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
     Y = t.tensor(curve_to_target(counts, n_traps), dtype=t.float32, device=model.dev)
@@ -328,9 +334,9 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
             if log_every and (k % log_every == 0 or k == steps - 1):
                 hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
         return hist
-    # The Adam kernel takes lr and the step as launch arguments, so a graph is
-    # captured per distinct (lr, step) would defeat replay; instead the graph
-    # holds the forward/backward pass only and Adam runs eagerly (10 launches).
+    # The Adam kernel takes lr and the step as launch arguments (a graph per
+    # distinct pair would defeat replay), so the graph holds the
+    # forward/backward pass and Adam runs eagerly (one launch).
     s = t.cuda.Stream()
     s.wait_stream(t.cuda.current_stream())
     with t.cuda.stream(s):
