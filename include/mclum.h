@@ -316,6 +316,11 @@ typedef struct mcl_adam_tensor {
 } mcl_adam_tensor;
 int mcl_adam_multi(const mcl_adam_tensor* tensors, int32_t n, float lr, float b1, float b2, float eps,
                    int32_t step, void* stream);
+/* The same with the learning rate (*lr) and the step (*step_base +
+ * step_offset, counting from 1) read on the device, so that a captured
+ * graph of several training steps replays with fresh values. */
+int mcl_adam_multi_dev(const mcl_adam_tensor* tensors, int32_t n, const float* lr, const int32_t* step_base,
+                       int32_t step_offset, float b1, float b2, float eps, void* stream);
 int mcl_f32_to_bf16(int64_t n, const float* x, void* y, void* stream);
 
 /* ---- CUDA graphs -------------------------------------------------------- */

@@ -228,7 +228,14 @@ struct AdamMulti {
 };
 
 __global__ void __launch_bounds__(256) adam_multi(const AdamMulti A, float lr, float b1, float b2, float eps,
-                                                  float bc1, float bc2) {
+                                                  float bc1, float bc2, const float* lr_dev,
+                                                  const int32_t* step_base, int32_t step_offset) {
+  if (lr_dev) {  // learning rate and step read on the device (graph replays)
+    lr = *lr_dev;
+    const float step = (float)(*step_base + step_offset);
+    bc1 = 1.0f - powf(b1, step);
+    bc2 = 1.0f - powf(b2, step);
+  }
   const mcl_adam_tensor& T = A.t[blockIdx.y];
   const int64_t n = (int64_t)T.rows * T.cols;
   __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(T.W);
@@ -589,7 +596,27 @@ extern "C" int mcl_adam_multi(const mcl_adam_tensor* tensors, int32_t n, float l
   }
   const float bc1 = 1.0f - powf(b1, (float)step), bc2 = 1.0f - powf(b2, (float)step);
   dim3 grid((unsigned)std::min<int64_t>((most + 255) / 256, 256), (unsigned)n);
-  adam_multi<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A, lr, b1, b2, eps, bc1, bc2);
+  adam_multi<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A, lr, b1, b2, eps, bc1, bc2, nullptr,
+                                                                        nullptr, 0);
+  MCL_CUDA_TRY(cudaGetLastError());
+  return MCL_OK;
+}
+
+extern "C" int mcl_adam_multi_dev(const mcl_adam_tensor* tensors, int32_t n, const float* lr,
+                                  const int32_t* step_base, int32_t step_offset, float b1, float b2, float eps,
+                                  void* stream) {
+  if (!tensors || n < 1 || n > 16 || !lr || !step_base) return MCL_EINVAL;
+  AdamMulti A;
+  int64_t most = 0;
+  for (int i = 0; i < n; ++i) {
+    const mcl_adam_tensor& t = tensors[i];
+    if (t.rows <= 0 || t.cols <= 0 || !t.p || !t.g || !t.m1 || !t.m2) return MCL_EINVAL;
+    A.t[i] = t;
+    most = std::max<int64_t>(most, (int64_t)t.rows * t.cols);
+  }
+  dim3 grid((unsigned)std::min<int64_t>((most + 255) / 256, 256), (unsigned)n);
+  adam_multi<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A, 0.0f, b1, b2, eps, 1.0f, 1.0f, lr,
+                                                                        step_base, step_offset);
   MCL_CUDA_TRY(cudaGetLastError());
   return MCL_OK;
 }

@@ -31,49 +31,14 @@ import numpy as np
 
 from . import _lib
 from . import surrogate as S
-from .schedule import C_TO_K
 
 FREE = 4  # E, log10 s, alpha, log10 rho'
 
 
 def pack_curves(params: np.ndarray, n_traps: int, id0: int = 0):
-    """Vectorised ``pack_host`` for the surrogate's curve family (one TL
-    segment per set): the same struct values ``surrogate.curve_spec`` gives."""
-    n = len(params)
-    E, log_s, alpha, log_rho, log_dose, log_beta = (params[:, i].astype(np.float64) for i in range(6))
-    beta = 10.0 ** log_beta
-    k = np.maximum(1, np.ceil(S.BIN_C / (beta * 0.1) - 1e-9).astype(np.int64))
-    dt = S.BIN_C / (beta * k)
-    a_eff = alpha * (1e-6 / 10.0 ** log_rho) ** (1.0 / 3.0)
-    filled = np.rint(n_traps * (1.0 - np.exp(-(10.0 ** log_dose) / S.D0_GY))).astype(np.int64)
-    sets = np.zeros(n, dtype=_lib.SET_DTYPE)
-    segs = np.zeros(n, dtype=_lib.SEG_DTYPE)
-    steps = S.N_BINS * k
-    ar = np.arange(n, dtype=np.int64)
-    sets["n_slots"] = n_traps
-    sets["n_filled"] = filled
-    sets["seg_begin"] = ar
-    sets["seg_count"] = 1
-    sets["n_bins"] = S.N_BINS
-    sets["set_id"] = (id0 + ar) & 0xFFFFFFFF
-    sets["bin_offset"] = ar * S.N_BINS
-    sets["slot_offset"] = ar * n_traps
-    sets["u_offset"] = 0
-    sets["total_steps"] = steps
-    sets["step_offset"] = np.concatenate([[0], np.cumsum(steps)[:-1]])
-    sets["E"], sets["s"], sets["alpha"], sets["k_b"] = E, 10.0 ** log_s, a_eff, 8.617333262145e-5
-    segs["n_steps"] = steps
-    segs["steps_per_bin"] = k
-    segs["bin_offset"] = 0
-    segs["flags"] = _lib.MCL_SEG_THERMAL
-    segs["dt"] = dt
-    segs["dt_growth"] = 1.0
-    segs["T0"] = C_TO_K
-    segs["beta"] = beta
-    b_off = np.arange(n + 1, dtype=np.int64) * S.N_BINS
-    s_off = np.arange(n + 1, dtype=np.int64) * n_traps
-    u_off = np.zeros(n + 1, dtype=np.int64)
-    return sets, segs, b_off, s_off, u_off
+    """Packed host arrays of the surrogate's curve family (one TL segment per
+    set), built column-wise: ``surrogate.pack_curves``."""
+    return S.pack_curves(params, id0, n_traps)
 
 
 def mc_curves(params: np.ndarray, n_traps: int, seed: int, id0: int = 0):

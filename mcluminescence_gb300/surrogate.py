@@ -67,6 +67,49 @@ def curve_spec(p: Sequence[float], set_id: int, n_traps: int = N_TRAPS) -> SetSp
                    segments=[seg], set_id=set_id, kind="tl_curve").finalize()
 
 
+def pack_curves(params: np.ndarray, id0: int = 0, n_traps: int = N_TRAPS):
+    """The packed host arrays (as ``batch.pack_host`` returns them) of the
+    sets ``curve_spec`` builds, computed column-wise for many parameter
+    vectors at once (no per-set Python objects)."""
+    from . import _lib as L
+    from .schedule import K_B
+    p = np.asarray(params, dtype=np.float64).reshape(-1, 6)
+    n = p.shape[0]
+    E, log_s, alpha, log_rho, log_dose, log_beta = (p[:, i] for i in range(6))
+    beta = 10.0 ** log_beta
+    k = np.maximum(1, np.ceil(BIN_C / (beta * 0.1) - 1e-9).astype(np.int64))
+    dt = BIN_C / (beta * k)
+    a_eff = alpha * (1e-6 / 10.0 ** log_rho) ** (1.0 / 3.0)
+    filled = np.rint(n_traps * (1.0 - np.exp(-(10.0 ** log_dose) / D0_GY))).astype(np.int64)
+    steps = N_BINS * k
+    segs = np.zeros(n, dtype=L.SEG_DTYPE)
+    segs["n_steps"] = steps
+    segs["steps_per_bin"] = k
+    segs["bin_offset"] = 0
+    segs["flags"] = L.MCL_SEG_THERMAL
+    segs["dt"] = dt
+    segs["dt_growth"] = 1.0
+    segs["T0"] = C_TO_K
+    segs["beta"] = beta
+    sets = np.zeros(n, dtype=L.SET_DTYPE)
+    sets["n_slots"] = n_traps
+    sets["n_filled"] = filled
+    sets["seg_begin"] = np.arange(n)
+    sets["seg_count"] = 1
+    sets["n_bins"] = N_BINS
+    sets["set_id"] = (id0 + np.arange(n, dtype=np.int64)) & 0xFFFFFFFF
+    b_off = np.arange(n + 1, dtype=np.int64) * N_BINS
+    s_off = np.arange(n + 1, dtype=np.int64) * n_traps
+    u_off = np.concatenate([[0], np.cumsum(n_traps * (1 + steps))]).astype(np.int64)
+    sets["bin_offset"] = b_off[:-1]
+    sets["slot_offset"] = s_off[:-1]
+    sets["u_offset"] = u_off[:-1]
+    sets["total_steps"] = steps
+    sets["step_offset"] = np.concatenate([[0], np.cumsum(steps)[:-1]]) if n else 0
+    sets["E"], sets["s"], sets["alpha"], sets["k_b"] = E, 10.0 ** log_s, a_eff, K_B
+    return sets, segs, b_off, s_off, u_off
+
+
 def simulate_curves(params: np.ndarray, seed: int, id0: int = 0, n_traps: int = N_TRAPS,
                     chunk: int = 65536, precision: str = "fp32") -> np.ndarray:
     """Monte Carlo glow curves (counts per bin, float32 [n][200]) on the GPU."""
@@ -75,9 +118,9 @@ def simulate_curves(params: np.ndarray, seed: int, id0: int = 0, n_traps: int = 
     out = np.zeros((len(params), N_BINS), dtype=np.float32)
     for c0 in range(0, len(params), chunk):
         sub = params[c0:c0 + chunk]
-        specs = [curve_spec(p, id0 + c0 + i, n_traps) for i, p in enumerate(sub)]
-        b = BernoulliBatch(specs, precision=precision, seed=seed, want_alive=False,
-                           block=128 if precision == "fp32" else 256, ept=8 if precision == "fp32" else 2)
+        b = BernoulliBatch(None, packed=pack_curves(sub, id0 + c0, n_traps), precision=precision, seed=seed,
+                           want_alive=False, block=128 if precision == "fp32" else 256,
+                           ept=8 if precision == "fp32" else 2)
         b.launch()
         torch.cuda.synchronize()
         out[c0:c0 + len(sub)] = b.result().lum.reshape(len(sub), N_BINS)
@@ -223,9 +266,7 @@ class SurrogateMLP:
                 self._gemm(_lib_EPI.F32, B, k, n, self.dZ[l], n, L.Wt, n, None, self.dY[l], k)
             dY, lddy = self.dY[l], k
 
-    def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
-        """One Adam step on every weight and bias (one launch)."""
-        self.step_count += 1
+    def _adam_tensors(self):
         if getattr(self, "_adam_arr", None) is None:
             ts = []
             for L in self.layers:
@@ -235,9 +276,23 @@ class SurrogateMLP:
                 ts.append(_lib.AdamTensor(L.b.data_ptr(), L.gb.data_ptr(), L.mb.data_ptr(), L.vb.data_ptr(),
                                           None, None, 1, n))
             self._adam_arr = (_lib.AdamTensor * len(ts))(*ts)
-        _lib.check(self.lib.mcl_adam_multi(C.cast(self._adam_arr, C.c_void_p), len(self._adam_arr), C.c_float(lr),
-                                           C.c_float(b1), C.c_float(b2), C.c_float(eps), self.step_count,
-                                           self._s()), "mcl_adam_multi")
+        return C.cast(self._adam_arr, C.c_void_p), len(self._adam_arr)
+
+    def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        """One Adam step on every weight and bias (one launch)."""
+        self.step_count += 1
+        arr, n = self._adam_tensors()
+        _lib.check(self.lib.mcl_adam_multi(arr, n, C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
+                                           self.step_count, self._s()), "mcl_adam_multi")
+
+    def adam_step_dev(self, lr_ptr: int, step_base_ptr: int, step_offset: int, b1: float = 0.9,
+                      b2: float = 0.999, eps: float = 1e-8) -> None:
+        """Adam with lr = *lr_ptr and step = *step_base_ptr + step_offset read
+        on the device (for captured multi-step graphs)."""
+        arr, n = self._adam_tensors()
+        _lib.check(self.lib.mcl_adam_multi_dev(arr, n, C.c_void_p(lr_ptr), C.c_void_p(step_base_ptr), step_offset,
+                                               C.c_float(b1), C.c_float(b2), C.c_float(eps), self._s()),
+                   "mcl_adam_multi_dev")
 
     def state_dict(self) -> dict:
         """FP32 master weights and biases (host tensors), for checkpoints."""
@@ -303,14 +358,14 @@ def generate_dataset(n: int, seed: int, id0: int = 0, n_traps: int = N_TRAPS):
 
 def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: int = 4000,
           lr: float = 2e-3, lr_final: float = 5e-5, seed: int = 0, log_every: int = 0,
-          n_traps: int = N_TRAPS, use_graph: bool = True) -> List[float]:
+          n_traps: int = N_TRAPS, use_graph: bool = True, graph_steps: int = 25) -> List[float]:
     """Adam on random mini-batches; cosine decay from lr to lr_final.
 
-    One step (batch gather, forward, loss, backward) is ~25 small kernels,
-    so it is captured once in a CUDA graph and replayed; Adam, whose learning
-    rate and step count are launch arguments, runs after each replay as one
-    multi-tensor launch.  Returns the loss (mean squared error of the log
-    curve) every log_every steps."""
+    One step (batch gather, forward, loss, backward, Adam) is ~25 small
+    kernels, so ``graph_steps`` steps are captured once in a CUDA graph and
+    replayed; Adam reads the learning rate and step count from device
+    memory.  Returns the loss (mean squared error of the log curve) about
+    every log_every steps."""
     t = model.torch
     X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
     Y = t.tensor(curve_to_target(counts, n_traps), dtype=t.float32, device=model.dev)
@@ -334,29 +389,45 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
             if log_every and (k % log_every == 0 or k == steps - 1):
                 hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
         return hist
-    # The Adam kernel takes lr and the step as launch arguments (a graph per
-    # distinct pair would defeat replay), so the graph holds the
-    # forward/backward pass and Adam runs eagerly (one launch).
+    # G steps per graph: batch indices for the G steps are drawn before each
+    # replay, and Adam reads its learning rate and step from device memory,
+    # so one capture serves the whole run.
+    G = max(1, min(graph_steps, steps))
+    lr_all = t.tensor(lrs, dtype=t.float32, device=model.dev)
+    lr_cur = t.empty(G, dtype=t.float32, device=model.dev)
+    base = t.zeros(1, dtype=t.int32, device=model.dev)
+    idxs = t.zeros((G, model.B), dtype=t.int64, device=model.dev)
     s = t.cuda.Stream()
     s.wait_stream(t.cuda.current_stream())
-    with t.cuda.stream(s):
-        idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
-        model.set_inputs(X.index_select(0, idx))
-        model.set_targets(Y.index_select(0, idx))
+    with t.cuda.stream(s):   # one eager forward/backward before the capture
+        model.set_inputs(X.index_select(0, idxs[0]))
+        model.set_targets(Y.index_select(0, idxs[0]))
         model.forward()
         model.backward()
     t.cuda.current_stream().wait_stream(s)
     g = t.cuda.CUDAGraph()
     with t.cuda.graph(g):
-        model.set_inputs(X.index_select(0, idx))
-        model.set_targets(Y.index_select(0, idx))
-        model.forward()
-        model.backward()
-    for k in range(steps):
-        idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
+        for j in range(G):
+            model.set_inputs(X.index_select(0, idxs[j]))
+            model.set_targets(Y.index_select(0, idxs[j]))
+            model.forward()
+            model.backward()
+            model.adam_step_dev(lr_cur[j:].data_ptr(), base.data_ptr(), j + 1)
+    k = 0
+    while k + G <= steps:
+        idxs.copy_(t.randint(0, X.shape[0], (G, model.B), generator=gen, device=model.dev))
+        lr_cur.copy_(lr_all[k:k + G])
+        base.fill_(model.step_count)
         g.replay()
-        model.adam_step(lr=lrs[k])
-        if log_every and (k % log_every == 0 or k == steps - 1):
+        model.step_count += G
+        k += G
+        if log_every and ((k - 1) // log_every != (k - 1 - G) // log_every or k == steps):
+            hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
+    while k < steps:          # the remainder, eagerly
+        idx.copy_(t.randint(0, X.shape[0], (model.B,), generator=gen, device=model.dev))
+        body(k)
+        k += 1
+        if log_every and (k % log_every == 0 or k == steps):
             hist.append(float(model.loss.item()) / (model.B * DIMS[-1]))
     model.check_errors()
     return hist
