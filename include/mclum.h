@@ -184,7 +184,9 @@ typedef struct mcl_k_args {
   uint32_t* mt_state;      /* MCL_RNG_MT19937: [625] key words + position, in/out */
   const double* obs_time;  /* MCL_LOOP_LAB_ISO: observation times (s), ascending */
   double* obs_ratio;       /* MCL_LOOP_LAB_ISO: electrons / N_e at each observation */
-  void* workspace;         /* global-memory arrays when they exceed shared memory */
+  void* workspace;         /* per-simulation regions at ws_offset (FP64 hole
+                              coordinates; all arrays when they exceed shared
+                              memory); >= workspace_bytes of mcl_k_validate   */
   int64_t workspace_bytes;
   uint64_t seed;           /* MCL_RNG_PHILOX key                               */
   int32_t n_sims;
@@ -193,7 +195,7 @@ typedef struct mcl_k_args {
   int32_t block;           /* 256 or 512                                       */
   int32_t e_cap_max;       /* largest e_cap / h_cap (from mcl_k_validate)      */
   int32_t h_cap_max;
-  int32_t arrays_in_smem;  /* 1: electron/hole arrays in shared memory (from mcl_k_validate) */
+  int32_t arrays_in_smem;  /* 1: per-electron arrays and FP32 hole copies in shared memory (from mcl_k_validate) */
   int32_t reserved;
 } mcl_k_args;
 
@@ -253,11 +255,11 @@ int mcl_b_run_static(const mcl_b_args* args, void* stream);
 int mcl_bench_philox(uint32_t* sink, int32_t grid, int32_t iters, uint64_t seed, void* stream);
 
 /* ---- reference-kinetics mode ----------------------------------------------- */
-/* Host validation; also reports whether the electron/hole arrays of the
+/* Host validation; also reports whether the per-electron arrays of the
  * largest simulation fit in shared memory (*arrays_in_smem), the workspace
- * bytes needed otherwise (*workspace_bytes; each simulation's arrays start at
- * its ws_offset) and the largest capacities, all to be copied into
- * mcl_k_args. */
+ * bytes needed (*workspace_bytes: the end of the last region, each of
+ * mcl_k_region_bytes at its ws_offset) and the largest capacities, all to be
+ * copied into mcl_k_args. */
 int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng, int32_t block,
                    int64_t n_uniforms, int32_t* arrays_in_smem, int64_t* workspace_bytes,
                    int32_t* e_cap_max, int32_t* h_cap_max);
@@ -266,6 +268,13 @@ int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng, int32_t b
  * IndexError, simulate.py:64) or a capacity is exceeded, MCL_EBUDGET when an
  * injected stream runs out, MCL_ENOHOLE for a nearest search over no holes. */
 int mcl_k_run(const mcl_k_args* args, void* stream);
+/* Bytes of simulation i's global-memory region at sims[i].ws_offset (the FP64
+ * hole coordinates, plus the per-electron arrays unless they live in shared
+ * memory); offsets must be multiples of 16.  mcl_k_arrays_fit_smem tells
+ * whether the per-electron arrays of the largest simulation fit in shared
+ * memory, which mcl_k_validate reports as arrays_in_smem. */
+int64_t mcl_k_region_bytes(int32_t e_cap, int32_t h_cap, int32_t arrays_in_smem);
+int32_t mcl_k_arrays_fit_smem(int32_t e_cap_max, int32_t h_cap_max);
 
 /* ---- surrogate network (no counterpart in the reference) ------------------ */
 /* The reference fits parameters by running the Monte Carlo for every

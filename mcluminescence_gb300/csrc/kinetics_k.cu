@@ -61,6 +61,11 @@ __device__ __forceinline__ bool better(double v2, int i2, double v1, int i1) {
   return v2 < v1 || (v2 == v1 && i2 < i1);
 }
 
+// Per-simulation state.  The "local" arrays live in shared memory when they
+// fit (global memory otherwise); the FP64 hole coordinates always live in the
+// simulation's global-memory region: the nearest-centre scans read FP32
+// copies scaled by the largest box side from the local arrays and touch the
+// FP64 values only for the few candidates the FP32 pass cannot exclude.
 struct Arrays {
   double *ex, *ey, *ez, *ed;  // electron coordinates, nearest distance
   double* u2;                 // the step's wait uniform of each electron
@@ -69,26 +74,35 @@ struct Arrays {
   int32_t* en;                // nearest hole index
   uint8_t* choice;            // E_loc choice of the current step
   int32_t* mlist;             // electrons to rescan after a removal
-  double *hx, *hy, *hz;       // hole coordinates
+  float *hxf, *hyf, *hzf;     // hole coordinates / largest box side, FP32
+  double *hx, *hy, *hz;       // hole coordinates (global memory)
+  double inv_l;               // 1 / largest box side
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline size_t arrays_bytes(int e_cap, int h_cap) {
+__host__ __device__ inline size_t local_bytes(int e_cap, int h_cap) {
   return align16(sizeof(double) * 5 * (size_t)e_cap) + align16(sizeof(float) * 2 * (size_t)e_cap) +
          align16(sizeof(int32_t) * (size_t)e_cap) + align16((size_t)e_cap) +
-         align16(sizeof(int32_t) * (size_t)e_cap) + align16(sizeof(double) * 3 * (size_t)h_cap);
+         align16(sizeof(int32_t) * (size_t)e_cap) + align16(sizeof(float) * 3 * (size_t)h_cap);
 }
 
-__device__ inline Arrays carve(unsigned char* base, int e_cap, int h_cap) {
+__host__ __device__ inline size_t hole64_bytes(int h_cap) { return align16(sizeof(double) * 3 * (size_t)h_cap); }
+
+// Bytes of one simulation's global-memory region (at its ws_offset).
+__host__ __device__ inline size_t region_bytes(int e_cap, int h_cap, bool local_in_smem) {
+  return hole64_bytes(h_cap) + (local_in_smem ? 0 : local_bytes(e_cap, h_cap));
+}
+
+__device__ inline Arrays carve(unsigned char* local, int e_cap, int h_cap, unsigned char* region, int h_cap_sim) {
   Arrays A;
-  double* d = reinterpret_cast<double*>(base);
+  double* d = reinterpret_cast<double*>(local);
   A.ex = d;
   A.ey = d + e_cap;
   A.ez = d + 2 * e_cap;
   A.ed = d + 3 * e_cap;
   A.u2 = d + 4 * e_cap;
-  unsigned char* p = base + align16(sizeof(double) * 5 * (size_t)e_cap);
+  unsigned char* p = local + align16(sizeof(double) * 5 * (size_t)e_cap);
   A.edf = reinterpret_cast<float*>(p);
   A.lw = A.edf + e_cap;
   p += align16(sizeof(float) * 2 * (size_t)e_cap);
@@ -98,10 +112,15 @@ __device__ inline Arrays carve(unsigned char* base, int e_cap, int h_cap) {
   p += align16((size_t)e_cap);
   A.mlist = reinterpret_cast<int32_t*>(p);
   p += align16(sizeof(int32_t) * (size_t)e_cap);
-  double* h = reinterpret_cast<double*>(p);
+  float* f = reinterpret_cast<float*>(p);
+  A.hxf = f;
+  A.hyf = f + h_cap;
+  A.hzf = f + 2 * h_cap;
+  double* h = reinterpret_cast<double*>(region);
   A.hx = h;
-  A.hy = h + h_cap;
-  A.hz = h + 2 * h_cap;
+  A.hy = h + h_cap_sim;
+  A.hz = h + 2 * h_cap_sim;
+  A.inv_l = 1.0;
   return A;
 }
 
@@ -166,15 +185,41 @@ __device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v
   __syncthreads();
 }
 
+__device__ __forceinline__ float dsq3f(float ax, float ay, float az, float bx, float by, float bz) {
+  const float dx = ax - bx, dy = ay - by, dz = az - bz;
+  return (dx * dx + dy * dy) + dz * dz;
+}
+
+// FP32 prefilter of the nearest-centre searches.  Coordinates scaled by the
+// largest box side lie in [0, 1]; each FP32 coordinate is within 2^-24 of its
+// scaled FP64 value, so a scaled FP32 squared distance is within 24 * 2^-24
+// of the exact one.  A hole whose FP64 norm could be the minimum therefore
+// has an FP32 squared distance at most 48 * 2^-24 above the FP32 minimum; the
+// margin kSqMargin = 128 * 2^-24 keeps every such hole, and the exact FP64
+// comparison (the reference's order of operations, first index on ties)
+// decides among the candidates.
+constexpr float kSqMargin = 0x1p-17f;
+
+__device__ __forceinline__ float scaled(double x, double inv_l) { return __double2float_rn(__dmul_rn(x, inv_l)); }
+
 // Nearest hole of point p over holes [0, n_h): exact np.argmin of the norms.
-// Per thread: running best over its strided holes; sqrt only when the squared
-// distance does not exceed the best squared distance so far.
+// Pass 1: block minimum of the FP32 squared distances.  Pass 2: per thread a
+// running best over its strided candidates in FP64 (sqrt only when the
+// squared distance does not exceed the best so far), then the block argmin.
 template <int BLOCK>
 __device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, double py, double pz,
                               double& d_out, int& i_out) {
+  const float qx = scaled(px, A.inv_l), qy = scaled(py, A.inv_l), qz = scaled(pz, A.inv_l);
+  float m = INFINITY;
+  for (int h = threadIdx.x; h < n_h; h += BLOCK) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
+  double mv;
+  int dummy_i, dummy_a;
+  block_argmin<BLOCK>(sh, (double)m, 0, 0, mv, dummy_i, dummy_a);
+  const float thr = (float)mv + kSqMargin;
   double bsq = INFINITY, bd = INFINITY;
   int bi = INT_MAX;
   for (int h = threadIdx.x; h < n_h; h += BLOCK) {
+    if (!(dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]) <= thr)) continue;
     const double sq = dsq3(px, py, pz, A.hx[h], A.hy[h], A.hz[h]);
     if (sq <= bsq) {
       const double d = __dsqrt_rn(sq);
@@ -185,8 +230,7 @@ __device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, d
       }
     }
   }
-  int dummy;
-  block_argmin<BLOCK>(sh, bd, bi, 0, d_out, i_out, dummy);
+  block_argmin<BLOCK>(sh, bd, bi, 0, d_out, i_out, dummy_a);
 }
 
 // ---------------------------------------------------------------------------
@@ -305,9 +349,11 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       for (int k = tid; k < cnt; k += BLOCK) {
         const int idx = c0 + k, p = idx / 3, c = idx - 3 * p;
         const double u = value(S, k);
-        if (c == 0) X[p] = __dmul_rn(u, sx);
-        else if (c == 1) Y[p] = __dmul_rn(u, sy);
-        else Z[p] = __dmul_rn(u, sz);
+        const double v = __dmul_rn(u, c == 0 ? sx : (c == 1 ? sy : sz));
+        if (c == 0) X[p] = v;
+        else if (c == 1) Y[p] = v;
+        else Z[p] = v;
+        if (pass == 1) (c == 0 ? A.hxf : (c == 1 ? A.hyf : A.hzf))[p] = scaled(v, A.inv_l);
       }
       advance(S, cnt);
       __syncthreads();
@@ -319,9 +365,14 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     if (n_e > 0 && n_h == 0) status = MCL_ENOHOLE;
     for (int e = tid; e < n_e && status == MCL_OK; e += BLOCK) {
       const double px = A.ex[e], py = A.ey[e], pz = A.ez[e];
+      const float qx = scaled(px, A.inv_l), qy = scaled(py, A.inv_l), qz = scaled(pz, A.inv_l);
+      float m = INFINITY;
+      for (int h = 0; h < n_h; ++h) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
+      const float thr = m + kSqMargin;
       double bsq = INFINITY, bd = INFINITY;
       int bi = INT_MAX;
       for (int h = 0; h < n_h; ++h) {
+        if (!(dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]) <= thr)) continue;
         const double sq = dsq3(px, py, pz, A.hx[h], A.hy[h], A.hz[h]);
         if (sq <= bsq) {
           const double d = __dsqrt_rn(sq);
@@ -462,6 +513,9 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       A.hx[n_h] = nhx;
       A.hy[n_h] = nhy;
       A.hz[n_h] = nhz;
+      A.hxf[n_h] = scaled(nhx, A.inv_l);
+      A.hyf[n_h] = scaled(nhy, A.inv_l);
+      A.hzf[n_h] = scaled(nhz, A.inv_l);
     }
     log_event(step, 0, n_e, n_h);
     ++n_e;
@@ -480,7 +534,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
       const int k = base + tid;
       double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
-      float f0 = 0;
+      float f0 = 0, hxf0 = 0, hyf0 = 0, hzf0 = 0;
       int n0 = 0;
       if (k < ne_tail) {
         const int s = e_idx + 1 + k;
@@ -496,6 +550,9 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         hx0 = A.hx[s];
         hy0 = A.hy[s];
         hz0 = A.hz[s];
+        hxf0 = A.hxf[s];
+        hyf0 = A.hyf[s];
+        hzf0 = A.hzf[s];
       }
       __syncthreads();
       if (k < ne_tail) {
@@ -512,6 +569,9 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         A.hx[dst] = hx0;
         A.hy[dst] = hy0;
         A.hz[dst] = hz0;
+        A.hxf[dst] = hxf0;
+        A.hyf[dst] = hyf0;
+        A.hzf[dst] = hzf0;
       }
       __syncthreads();
     }
@@ -663,8 +723,11 @@ __global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap
       S.u_base = sm.u_offset;
       S.u_count = sm.u_count;
     }
-    unsigned char* base = SMEM_ARRAYS ? arr_base : reinterpret_cast<unsigned char*>(a.workspace) + sm.ws_offset;
-    const Arrays A = carve(base, SMEM_ARRAYS ? e_cap_max : sm.e_cap, SMEM_ARRAYS ? h_cap_max : sm.h_cap);
+    unsigned char* region = reinterpret_cast<unsigned char*>(a.workspace) + sm.ws_offset;
+    unsigned char* local = SMEM_ARRAYS ? arr_base : region + hole64_bytes(sm.h_cap);
+    Arrays A = carve(local, SMEM_ARRAYS ? e_cap_max : sm.e_cap, SMEM_ARRAYS ? h_cap_max : sm.h_cap, region,
+                     sm.h_cap);
+    A.inv_l = 1.0 / fmax(fmax(fmax(sm.L, sm.W), fmax(sm.H, sm.Lb)), fmax(fmax(sm.Wb, sm.Hb), 1e-300));
     if (run_sim<BLOCK>(a, si, sm, A, sh, S) != MCL_OK && a.sequential) break;
     // sequential runs share one injected stream: the next simulation starts
     // where this one stopped (like the reference's global RandomState)
@@ -707,24 +770,35 @@ extern "C" int mcl_k_validate(const mcl_k_sim* sims, int32_t n_sims, int32_t rng
     if (s.ws_offset % 16) return MCL_EINVAL;
     e_max = s.e_cap > e_max ? s.e_cap : e_max;
     h_max = s.h_cap > h_max ? s.h_cap : h_max;
-    const int64_t end = s.ws_offset + (int64_t)arrays_bytes(s.e_cap, s.h_cap);
+  }
+  const bool fits = kFixedSmem + local_bytes(e_max, h_max) <= kMaxSmem;
+  for (int32_t i = 0; i < n_sims; ++i) {
+    const int64_t end = sims[i].ws_offset + (int64_t)region_bytes(sims[i].e_cap, sims[i].h_cap, fits);
     ws = end > ws ? end : ws;
   }
-  const bool fits = kFixedSmem + arrays_bytes(e_max, h_max) <= kMaxSmem;
   if (arrays_in_smem) *arrays_in_smem = fits ? 1 : 0;
-  if (workspace_bytes) *workspace_bytes = fits ? 0 : ws;
+  if (workspace_bytes) *workspace_bytes = ws;
   if (e_cap_max) *e_cap_max = e_max;
   if (h_cap_max) *h_cap_max = h_max;
   return MCL_OK;
+}
+
+extern "C" int64_t mcl_k_region_bytes(int32_t e_cap, int32_t h_cap, int32_t arrays_in_smem) {
+  if (e_cap < 0 || h_cap < 0) return -1;
+  return (int64_t)region_bytes(e_cap, h_cap, arrays_in_smem != 0);
+}
+
+extern "C" int32_t mcl_k_arrays_fit_smem(int32_t e_cap_max, int32_t h_cap_max) {
+  return kFixedSmem + local_bytes(e_cap_max, h_cap_max) <= kMaxSmem ? 1 : 0;
 }
 
 namespace {
 template <int BLOCK>
 int launch_k(const mcl_k_args& a, cudaStream_t s) {
   const bool in_smem = a.arrays_in_smem != 0;
-  const size_t smem = kFixedSmem + (in_smem ? arrays_bytes(a.e_cap_max, a.h_cap_max) : 0);
+  const size_t smem = kFixedSmem + (in_smem ? local_bytes(a.e_cap_max, a.h_cap_max) : 0);
   if (smem > kMaxSmem) return MCL_ECAPACITY;
-  if (!in_smem && !a.workspace) return MCL_EINVAL;
+  if (!a.workspace) return MCL_EINVAL;
   auto fn = in_smem ? kk_kernel<BLOCK, true> : kk_kernel<BLOCK, false>;
   MCL_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = a.sequential ? 1 : a.n_sims;

@@ -144,14 +144,19 @@ def _fill_sims(params: Sequence[RunParams], steps: int, extra: int):
     return sims
 
 
-def _ws_offsets(sims: np.ndarray) -> int:
-    """Place each simulation's arrays in the workspace (global-memory mode)."""
+def _ws_offsets(lib, sims: np.ndarray) -> int:
+    """Place each simulation's global-memory region (sizes from the library)
+    back to back in the workspace; returns the total bytes."""
+    if len(sims) == 0:
+        return 0
+    fit = int(lib.mcl_k_arrays_fit_smem(int(sims["e_cap"].max()), int(sims["h_cap"].max())))
     off = 0
     for r in sims:
         r["ws_offset"] = off
-        e, h = int(r["e_cap"]), int(r["h_cap"])
-        a16 = lambda x: (x + 15) & ~15
-        off += a16(32 * e) + a16(4 * e) + a16(e) + a16(4 * e) + a16(24 * h)
+        nb = int(lib.mcl_k_region_bytes(int(r["e_cap"]), int(r["h_cap"]), fit))
+        if nb < 0:
+            raise ValueError("negative capacity")
+        off += nb
     return off
 
 
@@ -189,9 +194,11 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
         off += len(o)
     smem_flag, ws_need = C.c_int32(), C.c_int64()
     e_max, h_max = C.c_int32(), C.c_int32()
-    ws_bytes = _ws_offsets(sims)
+    ws_bytes = _ws_offsets(lib, sims)
     _lib.check(lib.mcl_k_validate(_lib.ptr(sims), n, code, block, n_u, C.byref(smem_flag),
                                   C.byref(ws_need), C.byref(e_max), C.byref(h_max)), "mcl_k_validate")
+    if ws_need.value > ws_bytes:
+        raise RuntimeError("workspace layout disagrees with the library")
     dev = torch.device("cuda")
     d_sims = torch.from_numpy(sims.view(np.uint8)).to(dev)
     rows = max(n * steps, 1)
@@ -213,8 +220,7 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
         st[:624] = np.asarray(keys, dtype=np.uint32)
         st[624] = int(pos)
         d_mt = torch.from_numpy(st.view(np.int32)).to(dev)
-    d_ws = (torch.zeros(max(ws_bytes, 16), dtype=torch.uint8, device=dev)
-            if not smem_flag.value else None)
+    d_ws = torch.empty(max(ws_need.value, 16), dtype=torch.uint8, device=dev)
     d_obs_t = d_obs_r = None
     if n_obs_tot:
         d_obs_t = torch.from_numpy(np.concatenate(obs_list)).to(dev)
