@@ -61,6 +61,15 @@ __device__ __forceinline__ bool better(double v2, int i2, double v1, int i1) {
   return v2 < v1 || (v2 == v1 && i2 < i1);
 }
 
+// Integer sort key of a double that is >= +0, +inf or NaN (distances, waits):
+// IEEE bit patterns of non-negative doubles order like their values, and NaN
+// maps below everything (np.argmin returns the first NaN).  Comparing keys
+// keeps the block reductions off the (slow) FP64 pipe.
+__device__ __forceinline__ long long argmin_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? LLONG_MIN : b;
+}
+
 // Per-simulation state.  The "local" arrays live in shared memory when they
 // fit (global memory otherwise); the FP64 hole coordinates always live in the
 // simulation's global-memory region: the nearest-centre scans read FP32
@@ -135,16 +144,20 @@ struct Shared {
   int n_mask;
 };
 
-// Block-wide argmin with np.argmin semantics; also ORs `any`.
+// Block-wide argmin with np.argmin semantics over values >= +0, +inf or NaN
+// (compared through argmin_key); also ORs `any`.
 template <int BLOCK>
 __device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v, int& out_i, int& out_any) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long k = argmin_key(v);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
+    const long long k2 = __shfl_down_sync(0xffffffffu, k, o);
     const double v2 = __shfl_down_sync(0xffffffffu, v, o);
     const int i2 = __shfl_down_sync(0xffffffffu, i, o);
     const int a2 = __shfl_down_sync(0xffffffffu, any, o);
-    if (better(v2, i2, v, i)) {
+    if (k2 < k || (k2 == k && i2 < i)) {
+      k = k2;
       v = v2;
       i = i2;
     }
@@ -161,12 +174,15 @@ __device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v
     v = lane < W ? sh.rv[lane] : INFINITY;
     i = lane < W ? sh.ri[lane] : INT_MAX;
     any = lane < W ? sh.ra[lane] : 0;
+    k = argmin_key(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
+      const long long k2 = __shfl_down_sync(0xffffffffu, k, o);
       const double v2 = __shfl_down_sync(0xffffffffu, v, o);
       const int i2 = __shfl_down_sync(0xffffffffu, i, o);
       const int a2 = __shfl_down_sync(0xffffffffu, any, o);
-      if (better(v2, i2, v, i)) {
+      if (k2 < k || (k2 == k && i2 < i)) {
+        k = k2;
         v = v2;
         i = i2;
       }
@@ -182,6 +198,40 @@ __device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v
   out_v = sh.best_v;
   out_i = sh.best_i;
   out_any = sh.any;
+  __syncthreads();
+}
+
+// Block-wide minimum of a float (NaN ignored, +inf if all are) and OR of flags.
+template <int BLOCK>
+__device__ void block_minf(Shared& sh, float v, int flags, float& out_v, int& out_flags) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    flags |= __shfl_down_sync(0xffffffffu, flags, o);
+  }
+  if (lane == 0) {
+    sh.ri[warp] = __float_as_int(v);
+    sh.ra[warp] = flags;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int W = BLOCK / 32;
+    v = lane < W ? __int_as_float(sh.ri[lane]) : INFINITY;
+    flags = lane < W ? sh.ra[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+      flags |= __shfl_down_sync(0xffffffffu, flags, o);
+    }
+    if (lane == 0) {
+      sh.best_v = (double)v;
+      sh.any = flags;
+    }
+  }
+  __syncthreads();
+  out_v = (float)sh.best_v;
+  out_flags = sh.any;
   __syncthreads();
 }
 
@@ -212,10 +262,10 @@ __device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, d
   const float qx = scaled(px, A.inv_l), qy = scaled(py, A.inv_l), qz = scaled(pz, A.inv_l);
   float m = INFINITY;
   for (int h = threadIdx.x; h < n_h; h += BLOCK) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
-  double mv;
-  int dummy_i, dummy_a;
-  block_argmin<BLOCK>(sh, (double)m, 0, 0, mv, dummy_i, dummy_a);
-  const float thr = (float)mv + kSqMargin;
+  float mv;
+  int dummy_a;
+  block_minf<BLOCK>(sh, m, 0, mv, dummy_a);
+  const float thr = mv + kSqMargin;
   double bsq = INFINITY, bd = INFINITY;
   int bi = INT_MAX;
   for (int h = threadIdx.x; h < n_h; h += BLOCK) {
@@ -315,6 +365,22 @@ __device__ __forceinline__ double value(const Source& S, int k) {
   return (d & 1) ? u53(r.z, r.w) : u53(r.x, r.y);
 }
 
+// The 53-bit integer m of uniform k (value = m * 2^-53 exactly) for the
+// generated streams; the injected stream has doubles only.
+__device__ __forceinline__ uint64_t bits53(const Source& S, int k) {
+  uint32_t a, b;
+  if (S.rng == MCL_RNG_MT19937) {
+    a = S.ring[(S.rd + 2u * k) & (kRing - 1)];
+    b = S.ring[(S.rd + 2u * k + 1u) & (kRing - 1)];
+  } else {
+    const uint64_t d = (uint64_t)(S.pos + k);
+    const uint4 r = philox4x32_10((uint32_t)(d >> 1), S.stream, (uint32_t)(d >> 33), kTagK, S.k0, S.k1);
+    a = (d & 1) ? r.z : r.x;
+    b = (d & 1) ? r.w : r.y;
+  }
+  return ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+}
+
 __device__ __forceinline__ void advance(Source& S, int n) {
   S.pos += n;
   if (S.rng == MCL_RNG_MT19937) S.rd += 2u * n;
@@ -405,10 +471,18 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
   auto waits = [&](double T, double& wmin, int& emin, int& any) -> int {
     const double kT = __dmul_rn(sm.k_b, T);
     const double rcb = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT)));
+    // Generated streams stay in integers: u < Retrap  <=>  m < ceil(Retrap 2^53)
+    // (exact: u = m 2^-53), and the wait uniform is kept as m until the exact
+    // pass needs it as a double.
+    const bool gen = S.rng != MCL_RNG_INJECTED;
+    const uint64_t r53 = sm.Retrap >= 1.0 ? (1ull << 53)
+                         : sm.Retrap > 0.0 ? (uint64_t)ceil(__dmul_rn(sm.Retrap, 9007199254740992.0)) : 0ull;
+    uint64_t* u2bits = reinterpret_cast<uint64_t*>(A.u2);
     for (int c0 = 0; c0 < n_e; c0 += kChunk) {
       const int cnt = min(kChunk, n_e - c0);
       if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
-      for (int k = tid; k < cnt; k += BLOCK) A.choice[c0 + k] = value(S, k) < sm.Retrap ? 1 : 0;
+      for (int k = tid; k < cnt; k += BLOCK)
+        A.choice[c0 + k] = (gen ? bits53(S, k) < r53 : value(S, k) < sm.Retrap) ? 1 : 0;
       advance(S, cnt);
       __syncthreads();
     }
@@ -424,12 +498,20 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
       for (int k = tid; k < cnt; k += BLOCK) {
         const int e = c0 + k;
-        const double u2 = value(S, k);
-        A.u2[e] = u2;
+        float uf;
+        if (gen) {
+          const uint64_t m = bits53(S, k);
+          u2bits[e] = m;
+          uf = __fmul_rn(__ull2float_rn(m), 0x1p-53f);  // = float(m 2^-53), both rounded once
+        } else {
+          const double u2 = value(S, k);
+          A.u2[e] = u2;
+          uf = __double2float_rn(u2);
+        }
         const float arg = (A.choice[e] ? c2 : c1) - af * A.edf[e];
         const float lrt = lb + arg;
         const float lrate = lrcb > -INFINITY ? fmaxf(lrcb, lrt) + log1pf(expf(-fabsf(lrcb - lrt))) : lrt;
-        const float E = -log1pf(-__double2float_rn(u2));
+        const float E = -log1pf(-uf);
         const float lw = logf(E) - lrate;
         A.lw[e] = lw;
         // FP64 over/underflow of the rate (life 0 or inf) is left to the exact path
@@ -440,11 +522,11 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       advance(S, cnt);
       __syncthreads();
     }
-    double lmin_d;
-    int dummy_i, allflags;
-    block_argmin<BLOCK>(sh, (double)lmin, 0, flags, lmin_d, dummy_i, allflags);
+    float lmin_b;
+    int allflags;
+    block_minf<BLOCK>(sh, lmin, flags, lmin_b, allflags);
     const bool exact_all = (allflags & 1) != 0;
-    const float thr = (float)lmin_d + 1e-3f;
+    const float thr = lmin_b + 1e-3f;
     double bv = INFINITY;
     int bi = INT_MAX, an = 0;
     for (int e = tid; e < n_e; e += BLOCK) {
@@ -453,7 +535,8 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       const double arg = __dadd_rn(__ddiv_rn(-E_loc, kT), -__dmul_rn(sm.alpha, A.ed[e]));
       const double rate = __dmul_rn(sm.b, exp(arg));
       const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
-      const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -A.u2[e])));
+      const double u2 = gen ? __dmul_rn(__ull2double_rn(u2bits[e]), 0x1p-53) : A.u2[e];
+      const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -u2)));
       an |= (w != 0.0);
       if (better(w, e, bv, bi)) {
         bv = w;
