@@ -83,6 +83,7 @@ struct Arrays {
   int32_t* en;                // nearest hole index
   uint8_t* choice;            // E_loc choice of the current step
   int32_t* mlist;             // electrons to rescan after a removal
+  float *exf, *eyf, *ezf;     // electron coordinates / largest box side, FP32
   float *hxf, *hyf, *hzf;     // hole coordinates / largest box side, FP32
   double *hx, *hy, *hz;       // hole coordinates (global memory)
   double inv_l;               // 1 / largest box side
@@ -93,7 +94,8 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 __host__ __device__ inline size_t local_bytes(int e_cap, int h_cap) {
   return align16(sizeof(double) * 5 * (size_t)e_cap) + align16(sizeof(float) * 2 * (size_t)e_cap) +
          align16(sizeof(int32_t) * (size_t)e_cap) + align16((size_t)e_cap) +
-         align16(sizeof(int32_t) * (size_t)e_cap) + align16(sizeof(float) * 3 * (size_t)h_cap);
+         align16(sizeof(int32_t) * (size_t)e_cap) + align16(sizeof(float) * 3 * (size_t)e_cap) +
+         align16(sizeof(float) * 3 * (size_t)h_cap);
 }
 
 __host__ __device__ inline size_t hole64_bytes(int h_cap) { return align16(sizeof(double) * 3 * (size_t)h_cap); }
@@ -121,6 +123,11 @@ __device__ inline Arrays carve(unsigned char* local, int e_cap, int h_cap, unsig
   p += align16((size_t)e_cap);
   A.mlist = reinterpret_cast<int32_t*>(p);
   p += align16(sizeof(int32_t) * (size_t)e_cap);
+  float* g = reinterpret_cast<float*>(p);
+  A.exf = g;
+  A.eyf = g + e_cap;
+  A.ezf = g + 2 * e_cap;
+  p += align16(sizeof(float) * 3 * (size_t)e_cap);
   float* f = reinterpret_cast<float*>(p);
   A.hxf = f;
   A.hyf = f + h_cap;
@@ -142,6 +149,10 @@ struct Shared {
   int best_i;
   int any;
   int n_mask;
+  // per-step scalars, computed once (thread 0) instead of by every warp:
+  // GB300's FP64 pipe is narrow, so redundant FP64 work costs real time
+  double kT, rcb, dt_fill;
+  float c1, c2, lrcb;
 };
 
 // Block-wide argmin with np.argmin semantics over values >= +0, +inf or NaN
@@ -257,9 +268,8 @@ __device__ __forceinline__ float scaled(double x, double inv_l) { return __doubl
 // running best over its strided candidates in FP64 (sqrt only when the
 // squared distance does not exceed the best so far), then the block argmin.
 template <int BLOCK>
-__device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, double py, double pz,
-                              double& d_out, int& i_out) {
-  const float qx = scaled(px, A.inv_l), qy = scaled(py, A.inv_l), qz = scaled(pz, A.inv_l);
+__device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, double py, double pz, float qx,
+                              float qy, float qz, double& d_out, int& i_out) {
   float m = INFINITY;
   for (int h = threadIdx.x; h < n_h; h += BLOCK) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
   float mv;
@@ -294,7 +304,8 @@ struct Source {
   // Philox
   uint32_t k0, k1, stream;
   // MT19937 (shared memory)
-  uint32_t* mt;    // 624 key words
+  uint32_t* mt;    // 624 key words (current state)
+  uint32_t* mt2;   // the other state buffer
   uint32_t* ring;  // kRing tempered words
   uint32_t rd, wr;  // ring positions (identical in every thread)
   int64_t pos;     // doubles consumed in this simulation
@@ -313,28 +324,32 @@ __device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
   return y;
 }
 
-// One MT19937 state transition (Matsumoto & Nishimura 1998) by the whole CTA:
+// One MT19937 state transition (Matsumoto & Nishimura 1998) by the whole CTA,
+// from `cur` into `nxt` (two buffers, so no read/write hazards inside a
+// phase), each new word tempered straight into the output ring at wr + i:
 // indices [0,227) read only old words, [227,454) and [454,623) read words
-// updated 227 places earlier, 623 reads the new words 0 and 396.
+// updated 227 places earlier, 623 reads the new words 0 and 396.  Three
+// block barriers per 624 words.
 template <int BLOCK>
-__device__ void mt_twist(uint32_t* mt) {
-  const int t = threadIdx.x;
-  uint32_t v = 0;
-  if (t < kMtN - kMtM) v = mt_mix(mt[t], mt[t + 1], mt[t + kMtM]);
+__device__ void mt_twist(const uint32_t* cur, uint32_t* nxt, uint32_t* ring, uint32_t wr) {
+  constexpr int D = kMtN - kMtM;  // 227
+  for (int i = threadIdx.x; i < D; i += BLOCK) {
+    const uint32_t v = mt_mix(cur[i], cur[i + 1], cur[i + kMtM]);
+    nxt[i] = v;
+    ring[(wr + i) & (kRing - 1)] = mt_temper(v);
+  }
   __syncthreads();
-  if (t < kMtN - kMtM) mt[t] = v;
+  for (int i = D + threadIdx.x; i < 2 * D; i += BLOCK) {
+    const uint32_t v = mt_mix(cur[i], cur[i + 1], nxt[i - D]);
+    nxt[i] = v;
+    ring[(wr + i) & (kRing - 1)] = mt_temper(v);
+  }
   __syncthreads();
-  const int i1 = t + (kMtN - kMtM);
-  if (i1 < 2 * (kMtN - kMtM)) v = mt_mix(mt[i1], mt[i1 + 1], mt[i1 - (kMtN - kMtM)]);
-  __syncthreads();
-  if (i1 < 2 * (kMtN - kMtM)) mt[i1] = v;
-  __syncthreads();
-  const int i2 = t + 2 * (kMtN - kMtM);
-  if (i2 < kMtN - 1) v = mt_mix(mt[i2], mt[i2 + 1], mt[i2 - (kMtN - kMtM)]);
-  __syncthreads();
-  if (i2 < kMtN - 1) mt[i2] = v;
-  __syncthreads();
-  if (t == 0) mt[kMtN - 1] = mt_mix(mt[kMtN - 1], mt[0], mt[kMtM - 1]);
+  for (int i = 2 * D + threadIdx.x; i < kMtN; i += BLOCK) {
+    const uint32_t v = mt_mix(cur[i], i == kMtN - 1 ? nxt[0] : cur[i + 1], nxt[i - D]);
+    nxt[i] = v;
+    ring[(wr + i) & (kRing - 1)] = mt_temper(v);
+  }
   __syncthreads();
 }
 
@@ -345,10 +360,11 @@ __device__ bool ensure(Source& S, int n) {
   if (S.rng == MCL_RNG_INJECTED) return S.pos + n <= S.u_count;
   if (S.rng != MCL_RNG_MT19937) return true;
   while ((int)(S.wr - S.rd) < 2 * n) {
-    mt_twist<BLOCK>(S.mt);
-    for (int k = threadIdx.x; k < kMtN; k += BLOCK) S.ring[(S.wr + k) & (kRing - 1)] = mt_temper(S.mt[k]);
+    mt_twist<BLOCK>(S.mt, S.mt2, S.ring, S.wr);
+    uint32_t* t = S.mt;
+    S.mt = S.mt2;
+    S.mt2 = t;
     S.wr += kMtN;
-    __syncthreads();
   }
   return true;
 }
@@ -420,6 +436,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         else if (c == 1) Y[p] = v;
         else Z[p] = v;
         if (pass == 1) (c == 0 ? A.hxf : (c == 1 ? A.hyf : A.hzf))[p] = scaled(v, A.inv_l);
+        else (c == 0 ? A.exf : (c == 1 ? A.eyf : A.ezf))[p] = scaled(v, A.inv_l);
       }
       advance(S, cnt);
       __syncthreads();
@@ -431,7 +448,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     if (n_e > 0 && n_h == 0) status = MCL_ENOHOLE;
     for (int e = tid; e < n_e && status == MCL_OK; e += BLOCK) {
       const double px = A.ex[e], py = A.ey[e], pz = A.ez[e];
-      const float qx = scaled(px, A.inv_l), qy = scaled(py, A.inv_l), qz = scaled(pz, A.inv_l);
+      const float qx = A.exf[e], qy = A.eyf[e], qz = A.ezf[e];
       float m = INFINITY;
       for (int h = 0; h < n_h; ++h) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
       const float thr = m + kSqMargin;
@@ -468,9 +485,20 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
   // non-finite FP32 score or a rate near FP64 over/underflow sends the whole
   // step through the exact FP64 path.  wait != 0 (np.any) holds exactly when
   // some log-wait is above -inf, as -inf means U == 0.
+  const float af = __double2float_rn(sm.alpha);
+  const float lb = __double2float_rn(log(sm.b));
   auto waits = [&](double T, double& wmin, int& emin, int& any) -> int {
-    const double kT = __dmul_rn(sm.k_b, T);
-    const double rcb = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT)));
+    if (tid == 0) {
+      const double kT0 = __dmul_rn(sm.k_b, T);
+      const double rcb0 = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT0)));
+      sh.kT = kT0;
+      sh.rcb = rcb0;
+      sh.c1 = __double2float_rn(__ddiv_rn(-sm.E_loc_1, kT0));
+      sh.c2 = __double2float_rn(__ddiv_rn(-sm.E_loc_2, kT0));
+      sh.lrcb = rcb0 > 0.0 ? __double2float_rn(log(rcb0)) : -INFINITY;
+    }
+    __syncthreads();
+    const double kT = sh.kT, rcb = sh.rcb;
     // Generated streams stay in integers: u < Retrap  <=>  m < ceil(Retrap 2^53)
     // (exact: u = m 2^-53), and the wait uniform is kept as m until the exact
     // pass needs it as a double.
@@ -486,11 +514,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       advance(S, cnt);
       __syncthreads();
     }
-    const float c1 = __double2float_rn(__ddiv_rn(-sm.E_loc_1, kT));
-    const float c2 = __double2float_rn(__ddiv_rn(-sm.E_loc_2, kT));
-    const float af = __double2float_rn(sm.alpha);
-    const float lb = __double2float_rn(log(sm.b));
-    const float lrcb = rcb > 0.0 ? __double2float_rn(log(rcb)) : -INFINITY;
+    const float c1 = sh.c1, c2 = sh.c2, lrcb = sh.lrcb;
     float lmin = INFINITY;
     int flags = 0;  // bit 0: exact path needed; bit 1: some wait is non-zero
     for (int c0 = 0; c0 < n_e; c0 += kChunk) {
@@ -556,8 +580,10 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     dt_fill = 1e20;
     if (lam > 0.0) {
       if (!ensure<BLOCK>(S, 1)) return MCL_EBUDGET;
-      dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -value(S, 0))));
+      if (tid == 0) sh.dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -value(S, 0))));
       advance(S, 1);
+      __syncthreads();
+      dt_fill = sh.dt_fill;
     }
     return MCL_OK;
   };
@@ -585,11 +611,15 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     if (n_e + 1 > sm.e_cap || n_h + 1 > sm.h_cap) return MCL_ECAPACITY;
     double dn;
     int hn;
-    nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, dn, hn);  // OLD holes only
+    const float qx = scaled(nex, A.inv_l), qy = scaled(ney, A.inv_l), qz = scaled(nez, A.inv_l);
+    nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, qx, qy, qz, dn, hn);  // OLD holes only
     if (tid == 0) {
       A.ex[n_e] = nex;
       A.ey[n_e] = ney;
       A.ez[n_e] = nez;
+      A.exf[n_e] = qx;
+      A.eyf[n_e] = qy;
+      A.ezf[n_e] = qz;
       A.ed[n_e] = dn;
       A.edf[n_e] = __double2float_rn(dn);
       A.en[n_e] = hn;
@@ -617,7 +647,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     for (int base = 0; base < max(ne_tail, nh_tail); base += BLOCK) {
       const int k = base + tid;
       double x0 = 0, y0 = 0, z0 = 0, d0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
-      float f0 = 0, hxf0 = 0, hyf0 = 0, hzf0 = 0;
+      float f0 = 0, hxf0 = 0, hyf0 = 0, hzf0 = 0, exf0 = 0, eyf0 = 0, ezf0 = 0;
       int n0 = 0;
       if (k < ne_tail) {
         const int s = e_idx + 1 + k;
@@ -627,6 +657,9 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         d0 = A.ed[s];
         f0 = A.edf[s];
         n0 = A.en[s];
+        exf0 = A.exf[s];
+        eyf0 = A.eyf[s];
+        ezf0 = A.ezf[s];
       }
       if (k < nh_tail) {
         const int s = h_idx + 1 + k;
@@ -646,6 +679,9 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
         A.ed[dst] = d0;
         A.edf[dst] = f0;
         A.en[dst] = n0;
+        A.exf[dst] = exf0;
+        A.eyf[dst] = eyf0;
+        A.ezf[dst] = ezf0;
       }
       if (k < nh_tail) {
         const int dst = h_idx + k;
@@ -674,7 +710,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       const int e = A.mlist[m];
       double dn;
       int hn;
-      nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], dn, hn);
+      nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], A.exf[e], A.eyf[e], A.ezf[e], dn, hn);
       if (tid == 0) {
         A.ed[e] = dn;
         A.edf[e] = __double2float_rn(dn);
@@ -785,8 +821,9 @@ __global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap
   S.k0 = (uint32_t)a.seed;
   S.k1 = (uint32_t)(a.seed >> 32);
   S.mt = reinterpret_cast<uint32_t*>(smem);
-  S.ring = S.mt + 640;
-  unsigned char* arr_base = smem + sizeof(uint32_t) * (640 + kRing);
+  S.mt2 = S.mt + 640;
+  S.ring = S.mt + 1280;
+  unsigned char* arr_base = smem + sizeof(uint32_t) * (1280 + kRing);
   S.rd = S.wr = 0;
   if (a.rng == MCL_RNG_MT19937) {
     // load the key array and position; queue the untaken words of the current block
@@ -824,7 +861,7 @@ __global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap
   }
 }
 
-constexpr size_t kFixedSmem = sizeof(uint32_t) * (640 + kRing);
+constexpr size_t kFixedSmem = sizeof(uint32_t) * (1280 + kRing);
 constexpr size_t kMaxSmem = 220 * 1024;
 
 }  // namespace
