@@ -26,10 +26,10 @@
 //   FFMA gives d = 2^23 + h - c16 w (c16 = c 2^16 from the step table);
 //   d >= 2^23 + 1 proves u >= p, so nothing happens.  Each step keeps the
 //   minimum d over the thread's slots (3-input min).  In segments without
-//   filling one branch per 8-step block enters the exact test, which draws
-//   the uniform's low 16 bits from a separate Philox counter and checks
-//   u32 < ceil(p 2^32), p = -expm1f(-c w); it runs with probability
-//   ~ c w + 2^-16 per trial.  Filling segments branch once per step (a refill
+//   filling one branch per 8-step block enters the exact test, which checks
+//   u32 < ceil(p 2^32), p = -expm1f(-c w), drawing the uniform's low 16 bits
+//   from a separate Philox counter only when h sits on the threshold's upper
+//   half; it runs with probability ~ c w + 2^-16 per trial.  Filling segments branch once per step (a refill
 //   changes the next step's test).  Per trial the fast path is one byte
 //   permute, one FFMA and half a min, next to 1/8 of a Philox call (20
 //   32x32->64 multiplies on the FMA-heavy pipe, 20 3-input XORs);

@@ -89,20 +89,32 @@ __device__ __forceinline__ double r_prime_d(double u) { return cbrt(-log1p(-u));
 // Exact FP32-mode tests, kept out of line: they run on ~2e-5 of the trials.
 // The 32-bit uniform of a trial is (h << 16) | lo16: h is the 16-bit field the
 // fast test used, lo16 the low half of word 0 of philox(step, slot, set,
-// TAG_LO), drawn only here.
-__device__ __noinline__ uint32_t full_u32(uint32_t h, uint32_t kstep, uint32_t slot, uint32_t set_id,
-                                          const KParams& P) {
+// TAG_LO).  An event happens iff u32 < T, T = ceil(prob 2^32) (2^32 when
+// prob >= 1).  When every lo16 gives the same answer -- (h + 1) 2^16 <= T or
+// h 2^16 >= T -- the low half is not drawn: only h == T >> 16 needs it.  The
+// counter-based stream makes skipping a draw invisible to every other draw.
+__device__ __forceinline__ uint64_t threshold_u32(float prob) {
+  return prob >= 1.0f ? (1ull << 32) : (uint64_t)__float2uint_ru(__fmul_rn(prob, 4294967296.0f));
+}
+
+__device__ __noinline__ bool u32_below(uint32_t h, uint64_t T, uint32_t kstep, uint32_t slot, uint32_t set_id,
+                                       const KParams& P) {
+  const uint64_t lo_edge = (uint64_t)h << 16;
+  if (T >= lo_edge + 65536u) return true;
+  if (T <= lo_edge) return false;
   const uint4 r = philox_ks(kstep, slot, set_id, kTagLow, P);
-  return (h << 16) | (r.x & 0xffffu);
+  return (lo_edge | (r.x & 0xffffu)) < T;
 }
 
-__device__ __noinline__ bool escape_exact(uint32_t u32, float c, float w) {
-  const float p = -expm1f(-__fmul_rn(c, w));
-  return p >= 1.0f || u32 < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
+// p = -expm1f(-c w) for an escape
+__device__ __noinline__ bool escape_exact(uint32_t h, float c, float w, uint32_t kstep, uint32_t slot,
+                                          uint32_t set_id, const KParams& P) {
+  return u32_below(h, threshold_u32(-expm1f(-__fmul_rn(c, w))), kstep, slot, set_id, P);
 }
 
-__device__ __noinline__ bool threshold_exact(uint32_t u32, float q) {
-  return q >= 1.0f || u32 < __float2uint_ru(__fmul_rn(q, 4294967296.0f));
+__device__ __noinline__ bool threshold_exact(uint32_t h, float q, uint32_t kstep, uint32_t slot,
+                                             uint32_t set_id, const KParams& P) {
+  return u32_below(h, threshold_u32(q), kstep, slot, set_id, P);
 }
 
 __device__ __noinline__ float refill_w(uint32_t word, float alpha) {
@@ -198,8 +210,8 @@ struct SlotState {
 template <int EPT, int T>
 __device__ __forceinline__ bool try_escape(const KParams& P, const mcl_set& st, SlotState<EPT>& S, int i,
                                            uint32_t word, float c16, int64_t kstep, uint32_t* s_lum, int bin) {
-  const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
-  if (!escape_exact(u32, c16 * kInv16, S.w[i])) return false;
+  if (!escape_exact(field16<T>(word), c16 * kInv16, S.w[i], (uint32_t)kstep, S.slot[i], st.set_id, P))
+    return false;
   S.filled &= ~(1u << i);
   S.w[i] = 0.0f;
   atomicAdd(&s_lum[bin], 1u);
@@ -227,8 +239,7 @@ __device__ __forceinline__ void step_fill(const KParams& P, const mcl_set& st, S
         if ((S.filled >> i) & 1u) {
           try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin);
         } else if (S.slot[i] < (uint32_t)st.n_slots) {
-          const uint32_t u32 = full_u32(field16<T>(word), (uint32_t)kstep, S.slot[i], st.set_id, P);
-          if (threshold_exact(u32, q16 * kInv16)) {
+          if (threshold_exact(field16<T>(word), q16 * kInv16, (uint32_t)kstep, S.slot[i], st.set_id, P)) {
             const uint4 rr = philox_ks((uint32_t)kstep, S.slot[i], st.set_id, kTagRefill, P);
             S.w[i] = refill_w(rr.x, alpha);
             S.filled |= 1u << i;
