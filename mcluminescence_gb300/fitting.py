@@ -22,10 +22,9 @@ Poisson counting noise.
 """
 from __future__ import annotations
 
-import math
 import time
 from dataclasses import dataclass, field
-from typing import Callable, Dict, Optional
+from typing import Dict
 
 import numpy as np
 

@@ -16,7 +16,7 @@ from __future__ import annotations
 import copy
 import csv
 import os
-from typing import Any, Dict, List, Optional, Sequence, Tuple
+from typing import Any, Dict, List, Sequence, Tuple
 
 import numpy as np
 

@@ -21,7 +21,7 @@ half TL ramps and half isothermal holds, ragged 1e3..1e5 traps) and
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import List, Optional
 
 import numpy as np

@@ -7,7 +7,6 @@ pytestmark = pytest.mark.gpu
 
 
 def test_surrogate_fitting_needs_far_less_monte_carlo():
-    import torch
     from mcluminescence_gb300 import fitting as Fm, surrogate as S
     P, Cn = S.generate_dataset(250000, seed=21)
     m = S.SurrogateMLP(batch=2048, seed=1)

@@ -1,5 +1,4 @@
 """Host-side logic of the event-driven drop-in (no GPU needed)."""
-import numpy as np
 import pytest
 
 from golden_io import k_case, load_k

@@ -1,6 +1,5 @@
 """The oracle's presentation binning/smoothing against the reference's own
 functions (golden vectors from tests/golden/make_golden_post.py)."""
-import json
 import os
 
 import numpy as np
