@@ -264,7 +264,9 @@ def main():
                    "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ, "n_items": batch.n_items,
                    "l2": "flushed between passes (256 MB write, untimed)",
                    "parallelism": f"replicas x{world} (independent sets, no collective)"},
-        "e2e": e2e, "gpu_launches": a.steps, "clocks": clk, "roofline": roof,
+        # each replayed pass launches the rate-table pre-pass and the kinetics kernel
+        "e2e": e2e, "gpu_launches": 2 * a.steps,
+        "gpu_launches_per_step": {"kb_tables": 1, "kb_f32": 1}, "clocks": clk, "roofline": roof,
         "wall_s_timed": t_wall,
     }
     out["dose_fade_irsl"] = sequence_bench(a, rank)
