@@ -162,7 +162,7 @@ def _ws_offsets(lib, sims: np.ndarray) -> int:
 
 def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox", seed: int = 0,
                  mt_state=None, uniforms: Optional[np.ndarray] = None, sequential: Optional[bool] = None,
-                 block: int = 256, extra_capacity: int = 64, want_events: bool = True):
+                 block: Optional[int] = None, extra_capacity: int = 64, want_events: bool = True):
     """Run simulations on the GPU.  ``rng``: "philox" (independent streams,
     parallel), "mt19937" (one shared stream continuing from ``mt_state``, a
     numpy legacy state tuple, sequential) or "injected" (``uniforms``; shared
@@ -176,6 +176,10 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
             "mt19937": _lib.MCL_RNG_MT19937}[rng]
     if sequential is None:
         sequential = rng != "philox"
+    if block is None:
+        # one CTA walking the simulations in order gains from more threads per
+        # barrier-separated phase; independent simulations fill the GPU with 256
+        block = 512 if sequential else 256
     n = len(params)
     sims = _fill_sims(params, steps, extra_capacity)
     n_u = 0
@@ -275,7 +279,7 @@ def _raise_for(status: np.ndarray, steps: int):
 
 def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,
              dose_rate: Optional[float] = None, csv_path: Optional[str] = None,
-             block: int = 256, return_result: bool = False):
+             block: Optional[int] = None, return_result: bool = False):
     """GPU replacement of src/class/simulate.py:simulate.
 
     ``rng="numpy"`` continues numpy's global legacy RandomState (seeded with
@@ -364,7 +368,7 @@ class TLTrapSim:
     """
 
     def __init__(self, cfg: Any, *, e_ratio_start: Optional[float] = None, rng: str = "numpy",
-                 seed: Optional[int] = None, block: int = 256):
+                 seed: Optional[int] = None, block: Optional[int] = None):
         self.cfg = cfg
         self.mc = cfg["exp_type_fp"]
         self.phys = physics(cfg["physics_fp"])
