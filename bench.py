@@ -278,6 +278,7 @@ def main():
         pick, _ = cpu_sample(specs, a.cpu_seconds)
         v, wall, tr, cores = run_cpu(specs, pick, a.seed)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "value_per_core": v / max(cores, 1),
                                "sample": f"{len(pick)} of the {a.sets} sets ({tr:.3e} trials, "
                                          f"{wall:.1f} s wall), oracle FP64 numpy restatement, "
                                          f"one process per core"}

@@ -41,3 +41,33 @@ def test_default_config_is_the_reference_composition():
     if not os.path.isdir(conf):
         pytest.skip("reference conf/ not available")
     assert compose(conf) == default_config()
+
+
+@pytest.mark.parametrize("n_e,holes", [(200, 200), (2000, 2000), (20000, 20000)])
+def test_event_workspace_layout_matches_validation(n_e, holes):
+    """Host region offsets (library sizes) cover what validation asks for,
+    in shared-memory and global-memory modes alike."""
+    import ctypes as C
+    from mcluminescence_gb300 import _lib
+    from mcluminescence_gb300.config import default_config
+    from mcluminescence_gb300.kinetics import _fill_sims, _ws_offsets
+    lib = _lib.load()
+    cfg = default_config()
+    cfg["exp_type_fp"].update({"N_e": n_e, "holes": holes, "e_ratio_start": 1})
+    runs = initialize_runs(cfg)
+    params = [run_params(runs[r]) for r in runs]
+    sims = _fill_sims(params, 100, 64)
+    total = _ws_offsets(lib, sims)
+    smem, ws, em, hm = C.c_int32(), C.c_int64(), C.c_int32(), C.c_int32()
+    assert lib.mcl_k_validate(_lib.ptr(sims), len(sims), _lib.MCL_RNG_PHILOX, 256, 0, C.byref(smem), C.byref(ws),
+                              C.byref(em), C.byref(hm)) == 0
+    assert ws.value == total
+    assert smem.value == lib.mcl_k_arrays_fit_smem(em.value, hm.value)
+    offs = sims["ws_offset"].astype(int)
+    assert all(o % 16 == 0 for o in offs)
+    for i in range(len(sims)):
+        end = offs[i] + lib.mcl_k_region_bytes(int(sims[i]["e_cap"]), int(sims[i]["h_cap"]), smem.value)
+        assert end <= total
+        if i + 1 < len(sims):
+            assert end <= offs[i + 1]
+    assert (n_e <= 2000) == bool(smem.value)
