@@ -230,8 +230,8 @@ def _surrogate_curves(model, u, known_t):
     """Area-normalised surrogate curves of unit-cube candidates u [F][P][4]."""
     import torch
     F, P, _ = u.shape
-    lo = torch.tensor(S.LOW[:FREE], dtype=torch.float32, device="cuda")
-    hi = torch.tensor(S.HIGH[:FREE], dtype=torch.float32, device="cuda")
+    lo = S.dev_const("LOW_FREE", S.LOW[:FREE], torch.float32, u.device)
+    hi = S.dev_const("HIGH_FREE", S.HIGH[:FREE], torch.float32, u.device)
     x = lo + (hi - lo) * u
     full = torch.cat([x, known_t[:, None, :].expand(F, P, 2)], dim=2).reshape(F * P, 6)
     y = S.predict_t(model, full)

@@ -449,11 +449,25 @@ def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
     return out
 
 
+_DEV_CONST = {}
+
+
+def dev_const(name: str, values, dtype, device):
+    """A small constant array on the device, uploaded once (a fresh upload from
+    pageable host memory would stall the stream on every call)."""
+    import torch
+    key = (name, dtype, str(device))
+    t = _DEV_CONST.get(key)
+    if t is None:
+        t = torch.tensor(values, dtype=dtype, device=device)
+        _DEV_CONST[key] = t
+    return t
+
+
 def standardize_t(p):
     """Device version of ``standardize`` (torch tensor [n][6])."""
-    import torch
-    lo = torch.tensor(LOW, dtype=p.dtype, device=p.device)
-    hi = torch.tensor(HIGH, dtype=p.dtype, device=p.device)
+    lo = dev_const("LOW", LOW, p.dtype, p.device)
+    hi = dev_const("HIGH", HIGH, p.dtype, p.device)
     return 2.0 * (p - lo) / (hi - lo) - 1.0
 
 
