@@ -281,6 +281,7 @@ def fit_surrogate(prob: Problem, model: "S.SurrogateMLP", pop: int = 32, sur_gen
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     F = len(prob.known)
+    model = model.inference_copy(F * pop)   # every candidate of a generation in one forward pass
     thr = accept_factor * prob.floor
     best = torch.full((F,), float("inf"), device="cuda")
     open_idx = torch.arange(F, device="cuda")

@@ -189,6 +189,7 @@ class SurrogateMLP:
         self.loss = f32(1)
         self.tc_err = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.use_tcgen05 = True
+        self.training = True      # False: forward only (no transposed copies for backward)
         self.step_count = 0
 
     # -- plumbing -------------------------------------------------------------
@@ -221,7 +222,8 @@ class SurrogateMLP:
         x = t.zeros(self.B, IN_PAD, dtype=t.bfloat16, device=self.dev)
         x[:, :6] = x_std.to(t.bfloat16)
         self.x0.copy_(x)
-        self.x0t.copy_(x.t())
+        if self.training:
+            self.x0t.copy_(x.t())   # only the first layer's weight gradient reads it
 
     def set_targets(self, y: "torch.Tensor") -> None:
         self.target[:, :DIMS[-1]].copy_(y)
@@ -234,7 +236,7 @@ class SurrogateMLP:
             n, k = self.outs[l], self.ins[l]
             if l < len(self.layers) - 1:
                 self._gemm(_lib_EPI.BIAS_GELU, B, n, k, A, lda, L.Wb, k, L.b, self.Z[l], n,
-                           self.Y[l], n, self.Yt[l], B)
+                           self.Y[l], n, self.Yt[l] if self.training else None, B)
                 A, lda = self.Y[l], n
             else:
                 self._gemm(_lib_EPI.BIAS, B, n, k, A, lda, L.Wb, k, L.b, self.Z[l], n)
@@ -307,6 +309,15 @@ class SurrogateMLP:
             L.Wb.copy_(L.W.to(t.bfloat16))
             L.Wt.copy_(L.W.t().contiguous().to(t.bfloat16))
         self.step_count = int(st.get("step", 0))
+
+    def inference_copy(self, batch: int) -> "SurrogateMLP":
+        """A forward-only model with the same weights and a batch of ``batch``
+        rows (rounded up to 128), so that large candidate sets run in one pass."""
+        b = -(-int(batch) // 128) * 128
+        m = SurrogateMLP(batch=b, seed=0, device=str(self.dev))
+        m.load_state_dict(self.state_dict())
+        m.training = False
+        return m
 
     def input_grad(self) -> "torch.Tensor":
         """d loss / d standardized input (after backward(want_input_grad=True))."""
