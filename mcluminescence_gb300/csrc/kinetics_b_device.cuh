@@ -1,5 +1,6 @@
 // Device code of the Bernoulli kernels, shared by the translation units that
-// instantiate them (one per precision / CTA size, compiled in parallel).
+// instantiate them (one per FP32 launch shape and one for FP64, compiled in
+// parallel).
 // The method is described at the top of kinetics_b.cu.
 #pragma once
 
@@ -600,9 +601,10 @@ using KernelFn = void (*)(const KParams);
 
 }  // namespace
 
-// Kernel getters, one per translation unit.  `occupancy` 0/1 selects the
-// register-unconstrained build; other values select a build compiled for that
-// many resident CTAs per SM, where one exists.  nullptr = no such kernel.
+// Kernel getters, one per translation unit.  `occupancy` 0 selects the
+// default build; another value selects the build compiled for that many
+// resident CTAs per SM (fewer registers), where one exists.  nullptr = no
+// such kernel.
 KernelFn b_f32_128_e2(int occupancy);
 KernelFn b_f32_128_e4(int occupancy);
 KernelFn b_f32_128_e8(int occupancy);
