@@ -30,6 +30,13 @@
 // Distances follow np.linalg.norm's order sqrt((dx*dx + dy*dy) + dz*dz) with no
 // contraction; nearest searches compare squared distances and take the square
 // root only when it can decide (first index wins ties, like np.argmin).
+// GB300 runs FP64 at ~1/64 of the FP32 rate, so the FP64 arithmetic is kept to
+// what decides a result: nearest searches scan FP32 coordinates first and
+// evaluate FP64 norms only for candidates within a proven margin, the wait
+// filter scores electrons in FP32 and evaluates FP64 waits only near the
+// minimum, generated uniforms stay 53-bit integers until a double is needed,
+// reductions compare integer keys, and per-step scalars are computed once per
+// CTA.  Every result stays the reference's FP64 result.
 #include <climits>
 #include <cmath>
 
