@@ -305,9 +305,11 @@ def sequence_bench(a, rank):
     steps, sigma*Phi log-uniform 1e-3..1e-1 /s; traps start empty; uneven step
     counts) replayed from one captured CUDA graph."""
     import torch
-    from mcluminescence_gb300 import BernoulliBatch, schedule
+    from mcluminescence_gb300 import BernoulliBatch, autotune, schedule
     specs = schedule.batch_dose_fade_irsl(2048, seed=a.seed + 1 + 977 * rank)
-    b = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=128, ept=8, want_alive=True)
+    block, ept, occ = autotune.pick_bernoulli(specs, precision="fp32")
+    b = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, want_alive=True,
+                       occupancy=occ)
     st = torch.cuda.Stream()
     b.capture(st)
     for _ in range(2):
@@ -325,6 +327,7 @@ def sequence_bench(a, rank):
     ms = e0.elapsed_time(e1) / reps
     steps = [s.total_steps for s in specs]
     return {"sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": ms,
+            "block": block, "ept": ept, "occupancy_build": occ,
             "electron_steps_per_s": b.trials / (ms / 1e3), "steps_min": min(steps), "steps_max": max(steps),
             "events_per_pass": int(b.result().lum.sum())}
 
