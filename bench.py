@@ -280,6 +280,7 @@ def main():
         "wall_s_timed": t_wall,
     }
     out["dose_fade_irsl"] = sequence_bench(a, rank)
+    out["single_set_tl"] = single_set_bench(a, rank, world)
     if not a.no_k:
         out["reference_kinetics"] = kinetics_k_bench(a, rank, world)
     if not a.no_fit:
@@ -296,6 +297,37 @@ def main():
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def single_set_bench(a, rank, world):
+    """The plain single-set TL case (2,000 traps, E = 1.45 eV, s = 3.5e12,
+    0 -> 500 degC at 1 K/s, dt = 0.1 s, 1 degC bins) for alpha in {5, 10, 100}:
+    one launch each on the GPU (FP32 and the FP64 oracle-parity mode, latency
+    of a single small set) next to the FP64 CPU restatement on one core."""
+    import torch
+    from mcluminescence_gb300 import schedule, simulate_batch
+    out = {}
+    for alpha in (5.0, 10.0, 100.0):
+        sp = [schedule.single_tl_set(alpha=alpha, set_id=1 + rank)]
+        row = {}
+        for prec in ("fp32", "fp64"):
+            simulate_batch(sp, precision=prec, seed=a.seed)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = simulate_batch(sp, precision=prec, seed=a.seed)
+            torch.cuda.synchronize()
+            row[f"{prec}_ms"] = (time.perf_counter() - t0) * 1e3
+            row[f"{prec}_events"] = int(res.lum.sum())
+        if rank == 0 and world == 1 and not a.no_cpu_baseline:
+            from oracle import bernoulli as ob
+            t0 = time.perf_counter()
+            lum, _, _ = ob.run_set(sp[0].to_dict(), layout="f64", seed=a.seed)
+            row["cpu_port_1core_ms"] = (time.perf_counter() - t0) * 1e3
+            row["cpu_port_events"] = int(lum.sum())
+        out[f"alpha_{alpha:g}"] = row
+    out["trials"] = int(sp[0].trials)
+    out["timing"] = "wall clock around the public call (pack, upload, launch, read back)"
+    return out
 
 
 def sequence_bench(a, rank):
