@@ -413,6 +413,27 @@ def kinetics_k_bench(a, rank, world):
            "parallel_tl12_rate5": {"sims": n_par, "seconds": par_s, "electron_steps": par_esteps,
                                    "electron_steps_per_s": par_esteps / par_s,
                                    "events": int(rp.lum.sum())}}
+    # the reference's own CPU time on two golden cases (recorded when the
+    # fixtures were generated from the unmodified reference, one x86 core):
+    # the same inputs through simulate() here, outputs checked bit for bit
+    gold = np.load(os.path.join(HERE, "tests", "golden", "kinetics_k.npz"))
+    for case in ("tl12_full", "config1_shape"):
+        gcfg = json.loads(bytes(gold[f"{case}/cfg"]).decode())
+        seed = int(gold[f"{case}/seed"])
+        np.random.seed(seed)
+        K.simulate(gcfg)
+        torch.cuda.synchronize()
+        np.random.seed(seed)
+        t0 = time.perf_counter()
+        g_x, g_lum, g_ratio, _ = K.simulate(gcfg)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        ref_s = float(gold[f"{case}/wall_s"])
+        out[f"golden_{case}"] = {
+            "seconds": secs, "reference_cpu_seconds_recorded": ref_s, "speedup_vs_reference": ref_s / secs,
+            "bit_exact": bool(np.array_equal(g_lum, gold[f"{case}/lum"])
+                              and np.array_equal(g_ratio, gold[f"{case}/electron_ratio"])),
+            "steps": int(np.sum(gold[f"{case}/steps_taken"]))}
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         from oracle import kinetics_k as ok
         kr = ok.run_from_cfg(runs[3])          # the 20 K/s run (~1,200 steps)
