@@ -509,6 +509,7 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
     zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
 
     double w[EPT];
+    float wf[EPT];  // w rounded up to FP32 (the prefilter's bound)
     uint32_t slot[EPT];
     uint32_t filled = 0;
     const int64_t n = st.n_slots;
@@ -517,6 +518,7 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
       const int e = item.slot_begin + i * BLOCK + tid;
       slot[i] = (uint32_t)e;
       w[i] = 0.0;
+      wf[i] = 0.0f;
       if (e < st.n_slots) {
         double u;
         if (INJ) {
@@ -526,6 +528,7 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
           u = u53(r.x, r.y);
         }
         w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u)));
+        wf[i] = __double2float_ru(w[i]);
         if (e < st.n_filled) filled |= 1u << i;
       }
     }
@@ -559,25 +562,39 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
           }
           const double c = s_c[jj];
           const double qv = s_q[jj];
+          // FP32 prefilter (GB300 runs FP64 at ~1/64 of the FP32 rate): uf <= u
+          // (the top 24 bits of the 53-bit uniform, or the injected double
+          // rounded down) and xf >= p (c and w rounded up, product rounded up,
+          // times 1 + 2^-20 for expm1's last bit, as p = 1 - e^{-cw} <= cw);
+          // uf > xf proves u >= p, so the exact FP64 test runs only otherwise.
+          const float cf = __fmul_ru(__double2float_ru(c), 1.0f + 0x1p-20f);
+          const float qf = __double2float_ru(qv);
 #pragma unroll
           for (int i = 0; i < EPT; ++i) {
             if (slot[i] >= (uint32_t)st.n_slots) continue;
-            double u;
+            const bool full = (filled >> i) & 1u;
+            if (!full && !(!INJ && fill_on)) continue;
+            float uf;
+            double uinj = 0.0;
             if (INJ) {
-              u = a.uniforms[st.u_offset + n + k * n + slot[i]];
+              uinj = a.uniforms[st.u_offset + n + k * n + slot[i]];
+              uf = __double2float_rd(uinj);
             } else {
-              u = (j & 1) ? u53(r[i].z, r[i].w) : u53(r[i].x, r[i].y);
+              uf = __fmul_rn(__uint2float_rz(((j & 1) ? r[i].z : r[i].x) >> 8), 0x1p-24f);
             }
-            if ((filled >> i) & 1u) {
+            if (uf > (full ? __fmul_ru(cf, wf[i]) : qf)) continue;
+            const double u = INJ ? uinj : ((j & 1) ? u53(r[i].z, r[i].w) : u53(r[i].x, r[i].y));
+            if (full) {
               const double p = -expm1(__dmul_rn(-c, w[i]));
               if (u < p) {
                 filled &= ~(1u << i);
                 atomicAdd(&s_lum[bin], 1u);
                 if (a.fates) a.fates[st.slot_offset + slot[i]] = (int32_t)k;
               }
-            } else if (!INJ && fill_on && u < qv) {
+            } else if (u < qv) {
               const uint4 rr = philox_ks((uint32_t)k, slot[i], st.set_id, kTagRefill, P);
               w[i] = exp(__dmul_rn(-st.alpha, r_prime_d(u53(rr.x, rr.y))));
+              wf[i] = __double2float_ru(w[i]);
               filled |= 1u << i;
             }
           }
