@@ -51,7 +51,7 @@ def test_event_workspace_layout_matches_validation(n_e, holes):
     from mcluminescence_gb300 import _lib
     from mcluminescence_gb300.config import default_config
     from mcluminescence_gb300.kinetics import _fill_sims, _ws_offsets
-    lib = _lib.load()
+    lib = _lib.load(auto_build=True)
     cfg = default_config()
     cfg["exp_type_fp"].update({"N_e": n_e, "holes": holes, "e_ratio_start": 1})
     runs = initialize_runs(cfg)
