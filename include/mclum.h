@@ -290,8 +290,6 @@ int32_t mcl_k_arrays_fit_smem(int32_t e_cap_max, int32_t h_cap_max);
 int mcl_gemm_nt(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                 const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
                 int32_t ldy, void* Yt, int32_t ldyt, void* stream);
-/* dZ = dY * gelu'(Z) (or dY when gelu_on == 0) as bf16 in [M][N] and [N][M];
- * db[n] += sum_m dZ[m][n] (db must be cleared by the caller). */
 /* The same GEMM on the tcgen05 tensor cores (accumulator in tensor memory):
  * M multiple of 128, N of 64, K of 64.  *err is set to 1 if a completion wait
  * times out (the kernel then skips its epilogue and still frees its tensor
@@ -299,6 +297,8 @@ int mcl_gemm_nt(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A
 int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                    const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
                    int32_t ldy, void* Yt, int32_t ldyt, int32_t* err, void* stream);
+/* dZ = dY * gelu'(Z) (or dY when gelu_on == 0) as bf16 in [M][N] and [N][M];
+ * db[n] += sum_m dZ[m][n] (db must be cleared by the caller). */
 int mcl_act_backward(int32_t M, int32_t N, const float* dY, int32_t lddy, const float* Z, int32_t ldz,
                      int32_t gelu_on, void* dZ, int32_t lddz, void* dZt, int32_t lddzt, float* db,
                      void* stream);
