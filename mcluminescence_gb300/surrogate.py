@@ -244,7 +244,7 @@ class SurrogateMLP:
 
     def backward(self, want_input_grad: bool = False) -> None:
         """Gradients of the mean squared error (over batch and 200 bins)."""
-        t, B = self.torch, self.B
+        B = self.B
         self.loss.zero_()
         _lib.check(self.lib.mcl_mse_loss(B, OUT_PAD, DIMS[-1], self._p(self.Z[-1]), OUT_PAD,
                                          self._p(self.target), OUT_PAD, C.c_float(1.0 / (B * DIMS[-1])),

@@ -170,6 +170,7 @@ def test_fill_fade_irsl_sequence_fp64():
     for i, (lum, alive, fates) in enumerate(oracle_all(specs, "f64", 8)):
         assert np.array_equal(res.lum_of(i), lum), i
         assert np.array_equal(res.alive_of(i), alive), i
+        assert np.array_equal(res.fates_of(i), fates), i
 
 
 def test_fill_fade_irsl_sequence_fp32_fates():

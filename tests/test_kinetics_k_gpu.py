@@ -79,7 +79,7 @@ def test_philox_parallel_statistics_and_determinism():
     cfg["exp_type_fp"] = dict(cfg["exp_type_fp"], sims=64)
     (x1, l1, r1, _), = [simulate(cfg, rng="philox", seed=3)]
     x2, l2, r2, _ = simulate(cfg, rng="philox", seed=3)
-    assert np.array_equal(l1, l2) and np.array_equal(x1, x2)
+    assert np.array_equal(l1, l2) and np.array_equal(x1, x2) and np.array_equal(r1, r2)
     ref = case["lum"].sum(axis=0)          # (sims=2, runs=3) reference totals
     got = l1.sum(axis=0)                   # (64, 3)
     for r in range(3):
