@@ -133,7 +133,8 @@ typedef struct mcl_b_args {
   int32_t occupancy;       /* FP32 build: 0 = default; else resident CTAs per
                               SM the build targets (fewer registers): 4 at
                               block 256 / 8 at block 128 with ept 2, 3 at
-                              block 256 / 6 at block 128 with ept 4           */
+                              block 256 / 6 at block 128 with ept 4, 2 at
+                              block 256 / 4 at block 128 with ept 8           */
 } mcl_b_args;
 
 /* ---- reference-kinetics (event-driven) mode ----------------------------- */

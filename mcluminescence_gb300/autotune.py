@@ -18,7 +18,7 @@ from .schedule import SetSpec
 
 CANDIDATES = {
     "fp32": [(256, 4, 0), (256, 2, 0), (128, 4, 0), (128, 2, 0), (256, 8, 0), (128, 8, 0),
-             (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)],
+             (256, 8, 2), (128, 8, 4), (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)],
     "fp64": [(256, 1, 0), (256, 2, 0)],
 }
 CACHE = os.path.join(_build.LIBDIR, "autotune.json")

@@ -275,69 +275,92 @@ __device__ __forceinline__ void block_fill(const KParams& P, const mcl_set& st, 
 #undef MCL_STEP
 }
 
-// Exact tests of step T (index within its Philox block) of a segment without
-// filling, with d recomputed from the current state.  dcount gains 1 << 4T
-// per escape.
-template <int EPT, int T>
-__device__ __forceinline__ void escapes_of_step(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                                const uint4 (&r)[EPT], float c16, int64_t kstep,
-                                                uint32_t* s_lum, int bin, uint32_t& dcount) {
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    uint32_t word = word_of(r[i], T & 3);
-    // Recompute d here rather than keep the fast pass's 8 x EPT values live.
-    asm volatile("" : "+r"(word));
-    if (((S.filled >> i) & 1u) && __fmaf_rn(-c16, S.w[i], field_f<T>(word)) < kCand) {
-      if (try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin)) dcount += 1u << (4 * T);
-    }
+// Per-step tests of one trap over a Philox block of a segment without filling
+// (steps 0..nq-1): the Philox block is drawn again (the fast pass keeps only
+// a flag per trap), each step applies the FP32 test d = 2^23 + h - c16 w <
+// kCand and then the exact test.  Returns the step of the escape, or -1.  A
+// trap's fate depends only on its own uniforms, so testing the flagged traps
+// one after another gives the same escapes as testing step by step.
+__device__ __noinline__ int first_escape(const KParams& P, uint32_t set_id, uint32_t slot, float w, uint32_t blk,
+                                         const float* c16, int nq, int64_t kstep) {
+  const uint4 r = philox_ks(blk, slot, set_id, kTagStep, P);
+#define MCL_T(T)                                                                                  \
+  if ((T) < nq) {                                                                                 \
+    const uint32_t word = word_of(r, (T) & 3);                                                    \
+    const float c = c16[T];                                                                       \
+    if (__fmaf_rn(-c, w, field_f<T>(word)) < kCand &&                                             \
+        escape_exact(field16<T>(word), c * kInv16, w, (uint32_t)(kstep + (T)), slot, set_id, P))  \
+      return (T);                                                                                 \
   }
+  MCL_T(0) MCL_T(1) MCL_T(2) MCL_T(3) MCL_T(4) MCL_T(5) MCL_T(6) MCL_T(7)
+#undef MCL_T
+  return -1;
 }
 
+// Block-level integer prefilter of a segment without filling.  s_cm holds,
+// per 8-step block, cm = RU(max_t c16_t (1 + 2^-20)).  For a filled trap,
+// b = bits(RN(2^23 + 1 + cm w)) = 0x4B000000 + TI with TI = 1 + rint(cm w)
+// while cm w < 2^23 - 1.  An event at step t needs h < p 2^16 <= c16_t w
+// (1 + 2^-22) <= cm w (the tests above), hence h <= floor(cm w) < TI.  With
+// TI <= 0x7FFF both 16-bit fields of a Philox word are tested by one
+// subtraction r = word - TI (2^16 + 1): bit 15 of r & ~word is set iff
+// lo < TI, bit 31 iff hi < TI + [lo < TI] (a borrow only adds the case
+// hi == TI); a field with its top bit set is never below TI.  A trap whose
+// TI exceeds 0x7FFF (b > kHotBits: p near 1/2 or more, or a non-finite
+// rate) sends every filled trap of the block to the per-step tests.
+constexpr uint32_t kHotBits = 0x4B007FFFu;
+constexpr uint32_t kExp23 = 0x4B000000u;  // bits of 2^23
+constexpr float kCmScale = 1.0f + 0x1p-20f;
+
 // The steps of one Philox block of a segment without filling (8 steps; fewer
-// at the segment's end when FULL is false).  Traps only empty here, so a d
-// computed before an escape earlier in the block can only over-report
-// candidates: the fast pass evaluates d for all 8 steps with the state at the
-// block's start, keeps each step's minimum, and one branch per block enters
-// the exact tests of the steps whose minimum is below kCand.  The bin
-// bookkeeping then runs for the whole block: alive counts at bin ends inside
-// the block subtract the escapes up to that step, which dcount holds as 4-bit
-// counts per step (prefix sums by one multiply; EPT <= 8 keeps every nibble
-// below 16, as a trap escapes at most once here).
+// at the segment's end when FULL is false).  Traps only empty here, so flags
+// computed with the state at the block's start can only over-report: the
+// fast pass runs the integer prefilter above over the 8 steps of each slot
+// (one IADD and one LOP3 per word, i.e. per two trials) and keeps one flag
+// bit per slot; one branch per block sends the flagged filled traps to
+// first_escape.  The bin bookkeeping then runs for the whole block: alive
+// counts at bin ends inside the block subtract the escapes up to that step,
+// which dcount holds as 4-bit counts per step (prefix sums by one multiply;
+// EPT <= 8 keeps every nibble below 16, as a trap escapes at most once here).
 template <int EPT, bool FULL>
 __device__ __forceinline__ void block_nofill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                             uint32_t blk, const float* s_c, int jq, int nq, int64_t kstep,
-                                             uint32_t* s_lum, uint32_t* s_alive, int& bin, int& to_flush,
-                                             int spb, int seg_left) {
+                                             uint32_t blk, const float* s_c, const float* s_cm, int jq, int nq,
+                                             int64_t kstep, uint32_t* s_lum, uint32_t* s_alive, int& bin,
+                                             int& to_flush, int spb, int seg_left) {
   static_assert(EPT <= 8, "per-step escape counts are 4-bit fields");
-  uint4 r[EPT];
+  const float cm = s_cm[jq >> 3];
+  uint32_t mask = 0, hmax = 0;
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-  const float4 ca = *reinterpret_cast<const float4*>(s_c + jq);
-  const float4 cb = *reinterpret_cast<const float4*>(s_c + jq + 4);
-  const float c16[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
-  float m[8];
-#define MCL_MIN(T)                                                              \
-  if (FULL || (T) < nq) {                                                       \
-    float d[EPT];                                                               \
-    _Pragma("unroll") for (int i = 0; i < EPT; ++i)                             \
-        d[i] = __fmaf_rn(-c16[T], S.w[i], field_f<T>(word_of(r[i], (T) & 3)));  \
-    m[T] = min_all<EPT>(d);                                                     \
-  } else {                                                                      \
-    m[T] = kCand;                                                               \
+  for (int i = 0; i < EPT; ++i) {
+    const uint4 r = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
+    // empty traps (w = 0) get TI = 1 here; the mask drops them below
+    const uint32_t b = __float_as_uint(__fmaf_rn(cm, S.w[i], kCand));
+    hmax = max(hmax, b);
+    const uint32_t ntt = kExp23 - b - (b << 16);  // -(TI * 0x10001) mod 2^32
+    const uint32_t acc = ((r.x + ntt) & ~r.x) | ((r.y + ntt) & ~r.y) | ((r.z + ntt) & ~r.z) |
+                         ((r.w + ntt) & ~r.w);
+    if (acc & 0x80008000u) mask |= 1u << i;
   }
-  MCL_MIN(0) MCL_MIN(1) MCL_MIN(2) MCL_MIN(3) MCL_MIN(4) MCL_MIN(5) MCL_MIN(6) MCL_MIN(7)
-#undef MCL_MIN
+  if (hmax > kHotBits) mask = ~0u;
+  mask &= S.filled;
   const uint32_t alive0 = (uint32_t)__popc(S.filled);
   uint32_t dcount = 0;
-  if (min_all<8>(m) < kCand) {
-#define MCL_SLOW(T)                                                                           \
-  if ((FULL || (T) < nq) && m[T] < kCand) {                                                   \
-    int b = bin;                                                                              \
-    for (int tf = to_flush; (T) >= tf; tf += spb) ++b;                                        \
-    escapes_of_step<EPT, T>(P, st, S, r, c16[T], kstep + (T), s_lum, b, dcount);             \
-  }
-    MCL_SLOW(0) MCL_SLOW(1) MCL_SLOW(2) MCL_SLOW(3) MCL_SLOW(4) MCL_SLOW(5) MCL_SLOW(6) MCL_SLOW(7)
-#undef MCL_SLOW
+  if (mask) {
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      if ((mask >> i) & 1u) {
+        const int t = first_escape(P, st.set_id, S.slot[i], S.w[i], blk, s_c + jq, FULL ? 8 : nq, kstep);
+        if (t >= 0) {
+          S.filled &= ~(1u << i);
+          S.w[i] = 0.0f;
+          int b = bin;
+          for (int tf = to_flush; t >= tf; tf += spb) ++b;
+          atomicAdd(&s_lum[b], 1u);
+          if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)(kstep + t);
+          dcount += 1u << (4 * t);
+        }
+      }
+    }
   }
   const int n = FULL ? 8 : nq;
   if (to_flush > n) {
@@ -374,10 +397,27 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
   for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
     const int nj = min(kChunk, sg.n_steps - j0);
     __syncthreads();
-    for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
-      const float2 cq = tab[j0 + jj];
-      s_c[jj] = __fmul_rn(cq.x, 65536.0f);
-      s_q[jj] = __fmul_rn(cq.y, 65536.0f);
+    if (FILL) {
+      for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
+        const float2 cq = tab[j0 + jj];
+        s_c[jj] = __fmul_rn(cq.x, 65536.0f);
+        s_q[jj] = __fmul_rn(cq.y, 65536.0f);
+      }
+    } else {
+      // s_q holds the per-block bound cm of the integer prefilter here.  The
+      // trip count is uniform, so whole warps take part in the shuffles.
+      for (int j = 0; j < nj; j += BLOCK) {
+        const int jj = j + (int)threadIdx.x;
+        float c16 = 0.0f;
+        if (jj < nj) {
+          c16 = __fmul_rn(tab[j0 + jj].x, 65536.0f);
+          s_c[jj] = c16;
+        }
+        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 1));
+        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 2));
+        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 4));
+        if ((jj & 7) == 0 && jj < nj) s_q[jj >> 3] = __fmul_ru(c16, kCmScale);
+      }
     }
     __syncthreads();
     int jq = 0;
@@ -387,7 +427,7 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
         block_fill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush,
                               spb, sg.n_steps - (j0 + jq) - 1, alpha);
       else
-        block_nofill<EPT, true>(P, st, S, blk, s_c, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
+        block_nofill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
                                 sg.n_steps - (j0 + jq));
     }
     if (jq < nj) {  // the segment's last, partial Philox block
@@ -396,7 +436,7 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
         block_fill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
                                to_flush, spb, sg.n_steps - (j0 + jq) - 1, alpha);
       else
-        block_nofill<EPT, false>(P, st, S, blk, s_c, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
+        block_nofill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
                                  to_flush, spb, sg.n_steps - (j0 + jq));
     }
   }

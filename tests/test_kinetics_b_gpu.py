@@ -83,7 +83,8 @@ def test_fp32_fates_match_fp64_oracle_on_same_stream():
 
 
 @pytest.mark.parametrize("block,ept,occ", [(128, 2, 0), (256, 2, 0), (256, 8, 0), (128, 8, 0),
-                                            (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)])
+                                            (256, 8, 2), (128, 8, 4), (256, 4, 3), (128, 4, 6),
+                                            (256, 2, 4), (128, 2, 8)])
 def test_fp32_launch_shape_invariance(block, ept, occ):
     specs = mixed_specs()
     ref = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=256, ept=4)
