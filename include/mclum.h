@@ -135,6 +135,10 @@ typedef struct mcl_b_args {
                               block 256 / 8 at block 128 with ept 2, 3 at
                               block 256 / 6 at block 128 with ept 4, 2 at
                               block 256 / 4 at block 128 with ept 8           */
+  int32_t no_fill;         /* 1: no segment has fill_rate > 0; the FP32 launch
+                              then uses its build without the filling path
+                              (fewer registers), and a filling segment sets
+                              MCL_EINVAL in the status word                   */
 } mcl_b_args;
 
 /* ---- reference-kinetics (event-driven) mode ----------------------------- */

@@ -52,7 +52,7 @@ class BArgs(C.Structure):
         ("n_sets", C.c_int32), ("n_segs", C.c_int32), ("n_items", C.c_int32),
         ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
         ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
-        ("zero_outputs", C.c_int32), ("occupancy", C.c_int32),
+        ("zero_outputs", C.c_int32), ("occupancy", C.c_int32), ("no_fill", C.c_int32),
     ]
 
 

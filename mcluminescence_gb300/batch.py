@@ -146,6 +146,8 @@ class BernoulliBatch:
         self.n_items = int(n_items)
         self.max_bins = int(sets["n_bins"].max()) if len(sets) else 0
         self.host_sets, self.host_segs, self.host_items = sets, segs, items[:self.n_items]
+        # batches that never fill run the FP32 build without the filling path
+        self.no_fill = int(not np.any(segs["fill_rate"] > 0.0)) if len(segs) else 1
         self._trials = int(np.sum(n_slots * sets["total_steps"].astype(np.int64)))
         dev = torch.device(device)
         u8 = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).to(dev)
@@ -178,7 +180,7 @@ class BernoulliBatch:
         a.n_sets, a.n_segs, a.n_items = len(self.host_sets), len(self.host_segs), self.n_items
         a.slots_per_item, a.max_bins = self.block * self.ept, self.max_bins
         a.precision, a.rng, a.block, a.ept, a.grid = self.precision, self.rng, self.block, self.ept, self.grid
-        a.occupancy = self.occupancy
+        a.occupancy, a.no_fill = self.occupancy, self.no_fill
         a.zero_outputs = zero_outputs
         return a
 

@@ -50,8 +50,11 @@ KernelFn pick_kernel(const mcl_b_args& a) {
   if (a.precision == MCL_FP32) {
     if (a.rng != MCL_RNG_PHILOX) return nullptr;
     const int o = a.occupancy;
-    if (a.block == 128) return a.ept == 2 ? b_f32_128_e2(o) : a.ept == 4 ? b_f32_128_e4(o) : a.ept == 8 ? b_f32_128_e8(o) : nullptr;
-    if (a.block == 256) return a.ept == 2 ? b_f32_256_e2(o) : a.ept == 4 ? b_f32_256_e4(o) : a.ept == 8 ? b_f32_256_e8(o) : nullptr;
+    const bool f = a.no_fill == 0;
+    if (a.block == 128)
+      return a.ept == 2 ? b_f32_128_e2(o, f) : a.ept == 4 ? b_f32_128_e4(o, f) : a.ept == 8 ? b_f32_128_e8(o, f) : nullptr;
+    if (a.block == 256)
+      return a.ept == 2 ? b_f32_256_e2(o, f) : a.ept == 4 ? b_f32_256_e4(o, f) : a.ept == 8 ? b_f32_256_e8(o, f) : nullptr;
     return nullptr;
   }
   if (a.precision == MCL_FP64) return b_pick_f64(a.block, a.ept, a.rng == MCL_RNG_INJECTED);

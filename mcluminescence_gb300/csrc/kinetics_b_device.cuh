@@ -207,80 +207,72 @@ struct SlotState {
   uint32_t filled;     // bit i: slot i holds an electron
 };
 
-// Exact test of slot i at step T of the block for a trap that is filled.
-template <int EPT, int T>
-__device__ __forceinline__ bool try_escape(const KParams& P, const mcl_set& st, SlotState<EPT>& S, int i,
-                                           uint32_t word, float c16, int64_t kstep, uint32_t* s_lum, int bin) {
-  if (!escape_exact(field16<T>(word), c16 * kInv16, S.w[i], (uint32_t)kstep, S.slot[i], st.set_id, P))
-    return false;
-  S.filled &= ~(1u << i);
-  S.w[i] = 0.0f;
-  atomicAdd(&s_lum[bin], 1u);
-  if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)kstep;
-  return true;
+// Block-level integer prefilter.  When the CTA stages a chunk of the step
+// table it also stores, per 8-step block, cm = RU(max_t c16_t (1 + 2^-20))
+// and (filling segments) qm = RU(max_t q16_t (1 + 2^-20)).  For a filled
+// trap b = bits(RN(2^23 + 1 + cm w)) = 0x4B000000 + TI with TI = 1 +
+// rint(cm w) while cm w < 2^23 - 1; an empty trap of a filling segment uses
+// b = bits(RN(2^23 + 1 + qm)).  An escape at step t needs h < p 2^16 <=
+// c16_t w (1 + 2^-22) <= cm w (the tests above), a refill h < q16_t <= qm,
+// hence h <= floor(bound) < TI.  With TI <= 0x7FFF (b <= kHotBits) both
+// 16-bit fields of a Philox word are tested by one subtraction r = word -
+// TI (2^16 + 1): bit 15 of r & ~word is set iff lo < TI, bit 31 iff
+// hi < TI + [lo < TI] (a borrow only adds the case hi == TI); a field with
+// its top bit set is never below TI.  TI (2^16 + 1) is one byte permute of b,
+// whose low 16 bits are TI.  A trap with b > kHotBits (p or q near 1/2 or
+// more, or a non-finite rate) flags every trap of its thread's block.
+constexpr uint32_t kHotBits = 0x4B007FFFu;
+constexpr float kCmScale = 1.0f + 0x1p-20f;
+constexpr int kBlocksPerChunk = kChunk / 8;
+
+// Nonzero iff one of the 8 fields of Philox block r is below TI, b =
+// 0x4B000000 + TI.
+__device__ __forceinline__ uint32_t field_flags(const uint4& r, uint32_t b) {
+  const uint32_t tt = __byte_perm(b, 0u, 0x1010);  // TI * 0x10001 (TI < 2^16)
+  return (((r.x - tt) & ~r.x) | ((r.y - tt) & ~r.y) | ((r.z - tt) & ~r.z) | ((r.w - tt) & ~r.w)) &
+         0x80008000u;
 }
 
-// One step of a filling segment (index T within its Philox block) for all
-// EPT slots: filled traps may escape, empty ones may be refilled.
-template <int EPT, int T>
-__device__ __forceinline__ void step_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                          const uint4 (&r)[EPT], float c16, float q16, int64_t kstep,
-                                          uint32_t* s_lum, int bin, float alpha) {
-  float d[EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const float f = field_f<T>(word_of(r[i], T & 3));
-    d[i] = ((S.filled >> i) & 1u) ? __fmaf_rn(-c16, S.w[i], f) : __fsub_rn(f, q16);
+// Alive counts at the bin ends inside a block of n steps (the block's first
+// step is seg_left steps before the segment's end).  to_flush counts the
+// steps up to and including the one that ends the current bin; alive_at(t)
+// is the thread's filled count after step t.
+template <typename AliveAt>
+__device__ __forceinline__ void flush_block_bins(int n, uint32_t* s_alive, int& bin, int& to_flush, int spb,
+                                                 int seg_left, AliveAt alive_at) {
+  if (to_flush > n) {
+    to_flush -= n;
+    return;
   }
-  if (min_all<EPT>(d) < kCand) {
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      if (d[i] < kCand) {
-        const uint32_t word = word_of(r[i], T & 3);
-        if ((S.filled >> i) & 1u) {
-          try_escape<EPT, T>(P, st, S, i, word, c16, kstep, s_lum, bin);
-        } else if (S.slot[i] < (uint32_t)st.n_slots) {
-          if (threshold_exact(field16<T>(word), q16 * kInv16, (uint32_t)kstep, S.slot[i], st.set_id, P)) {
-            const uint4 rr = philox_ks((uint32_t)kstep, S.slot[i], st.set_id, kTagRefill, P);
-            S.w[i] = refill_w(rr.x, alpha);
-            S.filled |= 1u << i;
-          }
-        }
-      }
+  int t = to_flush - 1;  // block step that ends the current bin
+  for (;;) {
+    if (s_alive) warp_flush(alive_at(t), &s_alive[bin]);
+    ++bin;
+    const int next = min(spb, seg_left - t - 1);
+    if (next == 0) {  // the segment's last step
+      to_flush = 0;
+      return;
     }
+    if (t + next >= n) {
+      to_flush = t + next - n + 1;
+      return;
+    }
+    t += next;
   }
 }
 
-// The steps of one Philox block of a filling segment (8 steps; fewer at the
-// segment's end when FULL is false), one branch per step.
-template <int EPT, bool FULL>
-__device__ __forceinline__ void block_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
-                                           uint32_t blk, const float* s_c, const float* s_q, int jq,
-                                           int nq, int64_t kstep, uint32_t* s_lum, uint32_t* s_alive,
-                                           int& bin, int& to_flush, int spb, int remaining_after,
-                                           float alpha) {
-  uint4 r[EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) r[i] = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-#define MCL_STEP(T)                                                                             \
-  if (FULL || (T) < nq) {                                                                       \
-    step_fill<EPT, T>(P, st, S, r, s_c[jq + (T)], s_q[jq + (T)], kstep + (T), s_lum, bin, alpha); \
-    if (--to_flush == 0) {                                                                      \
-      if (s_alive) warp_flush((uint32_t)__popc(S.filled), &s_alive[bin]);                       \
-      ++bin;                                                                                    \
-      to_flush = min(spb, remaining_after - (T));                                               \
-    }                                                                                           \
-  }
-  MCL_STEP(0) MCL_STEP(1) MCL_STEP(2) MCL_STEP(3) MCL_STEP(4) MCL_STEP(5) MCL_STEP(6) MCL_STEP(7)
-#undef MCL_STEP
+// Bin of block step t (the current bin ends at step to_flush - 1).
+__device__ __forceinline__ int bin_of_step(int bin, int to_flush, int spb, int t) {
+  for (int tf = to_flush; t >= tf; tf += spb) ++bin;
+  return bin;
 }
 
-// Per-step tests of one trap over a Philox block of a segment without filling
-// (steps 0..nq-1): the Philox block is drawn again (the fast pass keeps only
-// a flag per trap), each step applies the FP32 test d = 2^23 + h - c16 w <
-// kCand and then the exact test.  Returns the step of the escape, or -1.  A
-// trap's fate depends only on its own uniforms, so testing the flagged traps
-// one after another gives the same escapes as testing step by step.
+// Per-step tests of one filled trap over a Philox block of a segment without
+// filling (steps 0..nq-1): the Philox block is drawn again (the fast pass
+// keeps only a flag per trap), each step applies the FP32 test d = 2^23 + h -
+// c16 w < kCand and then the exact test.  Returns the step of the escape, or
+// -1.  A trap's fate depends only on its own uniforms, so testing the flagged
+// traps one after another gives the same escapes as testing step by step.
 __device__ __noinline__ int first_escape(const KParams& P, uint32_t set_id, uint32_t slot, float w, uint32_t blk,
                                          const float* c16, int nq, int64_t kstep) {
   const uint4 r = philox_ks(blk, slot, set_id, kTagStep, P);
@@ -297,26 +289,11 @@ __device__ __noinline__ int first_escape(const KParams& P, uint32_t set_id, uint
   return -1;
 }
 
-// Block-level integer prefilter of a segment without filling.  s_cm holds,
-// per 8-step block, cm = RU(max_t c16_t (1 + 2^-20)).  For a filled trap,
-// b = bits(RN(2^23 + 1 + cm w)) = 0x4B000000 + TI with TI = 1 + rint(cm w)
-// while cm w < 2^23 - 1.  An event at step t needs h < p 2^16 <= c16_t w
-// (1 + 2^-22) <= cm w (the tests above), hence h <= floor(cm w) < TI.  With
-// TI <= 0x7FFF both 16-bit fields of a Philox word are tested by one
-// subtraction r = word - TI (2^16 + 1): bit 15 of r & ~word is set iff
-// lo < TI, bit 31 iff hi < TI + [lo < TI] (a borrow only adds the case
-// hi == TI); a field with its top bit set is never below TI.  A trap whose
-// TI exceeds 0x7FFF (b > kHotBits: p near 1/2 or more, or a non-finite
-// rate) sends every filled trap of the block to the per-step tests.
-constexpr uint32_t kHotBits = 0x4B007FFFu;
-constexpr uint32_t kExp23 = 0x4B000000u;  // bits of 2^23
-constexpr float kCmScale = 1.0f + 0x1p-20f;
-
 // The steps of one Philox block of a segment without filling (8 steps; fewer
 // at the segment's end when FULL is false).  Traps only empty here, so flags
 // computed with the state at the block's start can only over-report: the
-// fast pass runs the integer prefilter above over the 8 steps of each slot
-// (one IADD and one LOP3 per word, i.e. per two trials) and keeps one flag
+// fast pass runs the integer prefilter over the 8 steps of each slot (one
+// subtraction and one LOP3 per word, i.e. per two trials) and keeps one flag
 // bit per slot; one branch per block sends the flagged filled traps to
 // first_escape.  The bin bookkeeping then runs for the whole block: alive
 // counts at bin ends inside the block subtract the escapes up to that step,
@@ -333,13 +310,10 @@ __device__ __forceinline__ void block_nofill(const KParams& P, const mcl_set& st
 #pragma unroll
   for (int i = 0; i < EPT; ++i) {
     const uint4 r = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
-    // empty traps (w = 0) get TI = 1 here; the mask drops them below
+    // an empty trap (w = 0) gets TI = 1 here; the mask drops it below
     const uint32_t b = __float_as_uint(__fmaf_rn(cm, S.w[i], kCand));
     hmax = max(hmax, b);
-    const uint32_t ntt = kExp23 - b - (b << 16);  // -(TI * 0x10001) mod 2^32
-    const uint32_t acc = ((r.x + ntt) & ~r.x) | ((r.y + ntt) & ~r.y) | ((r.z + ntt) & ~r.z) |
-                         ((r.w + ntt) & ~r.w);
-    if (acc & 0x80008000u) mask |= 1u << i;
+    if (field_flags(r, b)) mask |= 1u << i;
   }
   if (hmax > kHotBits) mask = ~0u;
   mask &= S.filled;
@@ -353,70 +327,164 @@ __device__ __forceinline__ void block_nofill(const KParams& P, const mcl_set& st
         if (t >= 0) {
           S.filled &= ~(1u << i);
           S.w[i] = 0.0f;
-          int b = bin;
-          for (int tf = to_flush; t >= tf; tf += spb) ++b;
-          atomicAdd(&s_lum[b], 1u);
+          atomicAdd(&s_lum[bin_of_step(bin, to_flush, spb, t)], 1u);
           if (P.a.fates) P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)(kstep + t);
           dcount += 1u << (4 * t);
         }
       }
     }
   }
-  const int n = FULL ? 8 : nq;
-  if (to_flush > n) {
-    to_flush -= n;
-    return;
-  }
   const uint32_t cum = dcount * 0x11111111u;  // nibble t: escapes in steps 0..t
-  int t = to_flush - 1;                        // block step that ends the current bin
-  for (;;) {
-    if (s_alive) warp_flush(alive0 - ((cum >> (4 * t)) & 0xfu), &s_alive[bin]);
-    ++bin;
-    const int next = min(spb, seg_left - t - 1);
-    if (next == 0) {  // the segment's last step
-      to_flush = 0;
-      return;
-    }
-    if (t + next >= n) {
-      to_flush = t + next - n + 1;
-      return;
-    }
-    t += next;
-  }
+  flush_block_bins(FULL ? 8 : nq, s_alive, bin, to_flush, spb, seg_left,
+                   [&](int t) { return alive0 - ((cum >> (4 * t)) & 0xfu); });
 }
 
-// One segment of one work item (FP32).
+// Events of one trap over a Philox block of a filling segment (steps
+// 0..nq-1), step by step: a filled trap may escape (FP32 test, then the
+// exact test), an empty one in a real slot may be refilled (threshold q,
+// then a fresh w from its refill counter) -- the tests of the per-step
+// filling path, applied to one trap.  ev bits 0-7: escape steps; bits 8-15:
+// refill steps; bit 16: filled at the end; w: the trap's w at the end.
+struct FillEvents {
+  uint32_t ev;
+  float w;
+};
+
+__device__ __noinline__ FillEvents fill_events(const KParams& P, uint32_t set_id, uint32_t slot, bool real,
+                                               bool filled, float w, uint32_t blk, const float* c16,
+                                               const float* q16, int nq, int64_t kstep, float alpha) {
+  const uint4 r = philox_ks(blk, slot, set_id, kTagStep, P);
+  uint32_t ev = 0;
+#define MCL_T(T)                                                                                          \
+  if ((T) < nq) {                                                                                         \
+    const uint32_t word = word_of(r, (T) & 3);                                                            \
+    const float f = field_f<T>(word);                                                                     \
+    const uint32_t ks = (uint32_t)(kstep + (T));                                                          \
+    if (filled) {                                                                                         \
+      const float c = c16[T];                                                                             \
+      if (__fmaf_rn(-c, w, f) < kCand && escape_exact(field16<T>(word), c * kInv16, w, ks, slot, set_id, P)) { \
+        filled = false;                                                                                   \
+        w = 0.0f;                                                                                         \
+        ev |= 1u << (T);                                                                                  \
+      }                                                                                                   \
+    } else if (real) {                                                                                    \
+      const float q = q16[T];                                                                             \
+      if (__fsub_rn(f, q) < kCand && threshold_exact(field16<T>(word), q * kInv16, ks, slot, set_id, P)) { \
+        const uint4 rr = philox_ks(ks, slot, set_id, kTagRefill, P);                                      \
+        w = refill_w(rr.x, alpha);                                                                        \
+        filled = true;                                                                                    \
+        ev |= 0x100u << (T);                                                                              \
+      }                                                                                                   \
+    }                                                                                                     \
+  }
+  MCL_T(0) MCL_T(1) MCL_T(2) MCL_T(3) MCL_T(4) MCL_T(5) MCL_T(6) MCL_T(7)
+#undef MCL_T
+  return FillEvents{ev | (filled ? 0x10000u : 0u), w};
+}
+
+// The steps of one Philox block of a filling segment (8 steps; fewer at the
+// segment's end when FULL is false).  A trap that is not flagged by the
+// prefilter (filled: escape bound cm w; empty: refill bound qm) has no event
+// in the block, so it keeps its state and every later step of the block is
+// covered by the same test; a flagged trap goes to fill_events, which runs
+// all of the block's steps for it in order.  Refill and escape counts per step
+// (8-bit fields; at most EPT events per step and 4 EPT per block) give the
+// alive counts at bin ends inside the block.
+template <int EPT, bool FULL>
+__device__ __forceinline__ void block_fill(const KParams& P, const mcl_set& st, SlotState<EPT>& S,
+                                           uint32_t blk, const float* s_c, const float* s_q, const float* s_cm,
+                                           const float* s_qm, int jq, int nq, int64_t kstep, uint32_t* s_lum,
+                                           uint32_t* s_alive, int& bin, int& to_flush, int spb, int seg_left,
+                                           float alpha) {
+  const float cm = s_cm[jq >> 3];
+  const uint32_t bq = __float_as_uint(__fadd_rn(s_qm[jq >> 3], kCand));
+  uint32_t mask = 0, hmax = bq;
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    const uint4 r = philox_ks(blk, S.slot[i], st.set_id, kTagStep, P);
+    const uint32_t b = ((S.filled >> i) & 1u) ? __float_as_uint(__fmaf_rn(cm, S.w[i], kCand)) : bq;
+    hmax = max(hmax, b);
+    if (field_flags(r, b)) mask |= 1u << i;
+  }
+  if (hmax > kHotBits) mask = ~0u;
+  const uint32_t alive0 = (uint32_t)__popc(S.filled);
+  uint64_t ecnt = 0, rcnt = 0;
+  if (mask) {
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const bool filled = (S.filled >> i) & 1u;
+      const bool real = S.slot[i] < (uint32_t)st.n_slots;
+      if (((mask >> i) & 1u) && (filled || real)) {
+        const FillEvents o = fill_events(P, st.set_id, S.slot[i], real, filled, S.w[i], blk, s_c + jq, s_q + jq,
+                                         FULL ? 8 : nq, kstep, alpha);
+        if (o.ev & 0xffffu) {
+          S.w[i] = o.w;
+          S.filled = (o.ev & 0x10000u) ? (S.filled | (1u << i)) : (S.filled & ~(1u << i));
+          uint32_t esc = o.ev & 0xffu, ref = (o.ev >> 8) & 0xffu;
+          if (esc && P.a.fates)  // the last escape of the block
+            P.a.fates[st.slot_offset + S.slot[i]] = (int32_t)(kstep + (31 - __clz(esc)));
+          while (esc) {
+            const int t = __ffs(esc) - 1;
+            esc &= esc - 1;
+            atomicAdd(&s_lum[bin_of_step(bin, to_flush, spb, t)], 1u);
+            ecnt += 1ull << (8 * t);
+          }
+          while (ref) {
+            const int t = __ffs(ref) - 1;
+            ref &= ref - 1;
+            rcnt += 1ull << (8 * t);
+          }
+        }
+      }
+    }
+  }
+  uint64_t ecum = 0, rcum = 0;  // byte t: events in steps 0..t
+  if (ecnt | rcnt) {
+    ecum = ecnt * 0x0101010101010101ull;
+    rcum = rcnt * 0x0101010101010101ull;
+  }
+  flush_block_bins(FULL ? 8 : nq, s_alive, bin, to_flush, spb, seg_left, [&](int t) {
+    return alive0 + (uint32_t)((rcum >> (8 * t)) & 0xffu) - (uint32_t)((ecum >> (8 * t)) & 0xffu);
+  });
+}
+
+// One segment of one work item (FP32).  s_bm holds the per-block bounds of
+// the prefilter: cm at [0, kBlocksPerChunk), qm after it.
 template <int BLOCK, int EPT, bool FILL>
 __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st, const mcl_segment& sg,
                                             SlotState<EPT>& S, const float2* tab, float* s_c, float* s_q,
-                                            uint32_t* s_lum, uint32_t* s_alive, uint32_t bbase,
+                                            float* s_bm, uint32_t* s_lum, uint32_t* s_alive, uint32_t bbase,
                                             int64_t kglob, float alpha) {
   const int spb = sg.steps_per_bin;
   int bin = sg.bin_offset;
   int to_flush = min(spb, sg.n_steps);
+  float* s_cm = s_bm;
+  float* s_qm = s_bm + kBlocksPerChunk;
   for (int j0 = 0; j0 < sg.n_steps; j0 += kChunk) {
     const int nj = min(kChunk, sg.n_steps - j0);
     __syncthreads();
-    if (FILL) {
-      for (int jj = threadIdx.x; jj < nj; jj += BLOCK) {
+    // The trip count is uniform, so whole warps take part in the shuffles
+    // (a warp's lanes 8k..8k+7 hold one 8-step block).
+    for (int j = 0; j < nj; j += BLOCK) {
+      const int jj = j + (int)threadIdx.x;
+      float c16 = 0.0f, q16 = 0.0f;
+      if (jj < nj) {
         const float2 cq = tab[j0 + jj];
-        s_c[jj] = __fmul_rn(cq.x, 65536.0f);
-        s_q[jj] = __fmul_rn(cq.y, 65536.0f);
-      }
-    } else {
-      // s_q holds the per-block bound cm of the integer prefilter here.  The
-      // trip count is uniform, so whole warps take part in the shuffles.
-      for (int j = 0; j < nj; j += BLOCK) {
-        const int jj = j + (int)threadIdx.x;
-        float c16 = 0.0f;
-        if (jj < nj) {
-          c16 = __fmul_rn(tab[j0 + jj].x, 65536.0f);
-          s_c[jj] = c16;
+        c16 = __fmul_rn(cq.x, 65536.0f);
+        s_c[jj] = c16;
+        if (FILL) {
+          q16 = __fmul_rn(cq.y, 65536.0f);
+          s_q[jj] = q16;
         }
-        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 1));
-        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 2));
-        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, 4));
-        if ((jj & 7) == 0 && jj < nj) s_q[jj >> 3] = __fmul_ru(c16, kCmScale);
+      }
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        c16 = fmaxf(c16, __shfl_xor_sync(0xffffffffu, c16, o));
+        if (FILL) q16 = fmaxf(q16, __shfl_xor_sync(0xffffffffu, q16, o));
+      }
+      if ((jj & 7) == 0 && jj < nj) {
+        s_cm[jj >> 3] = __fmul_ru(c16, kCmScale);
+        if (FILL) s_qm[jj >> 3] = __fmul_ru(q16, kCmScale);
       }
     }
     __syncthreads();
@@ -424,19 +492,19 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
     for (; jq + 8 <= nj; jq += 8) {
       const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
       if (FILL)
-        block_fill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush,
-                              spb, sg.n_steps - (j0 + jq) - 1, alpha);
+        block_fill<EPT, true>(P, st, S, blk, s_c, s_q, s_cm, s_qm, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin,
+                              to_flush, spb, sg.n_steps - (j0 + jq), alpha);
       else
-        block_nofill<EPT, true>(P, st, S, blk, s_c, s_q, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush, spb,
-                                sg.n_steps - (j0 + jq));
+        block_nofill<EPT, true>(P, st, S, blk, s_c, s_cm, jq, 8, kglob + j0 + jq, s_lum, s_alive, bin, to_flush,
+                                spb, sg.n_steps - (j0 + jq));
     }
     if (jq < nj) {  // the segment's last, partial Philox block
       const uint32_t blk = bbase + (uint32_t)((j0 + jq) >> 3);
       if (FILL)
-        block_fill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
-                               to_flush, spb, sg.n_steps - (j0 + jq) - 1, alpha);
+        block_fill<EPT, false>(P, st, S, blk, s_c, s_q, s_cm, s_qm, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive,
+                               bin, to_flush, spb, sg.n_steps - (j0 + jq), alpha);
       else
-        block_nofill<EPT, false>(P, st, S, blk, s_c, s_q, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
+        block_nofill<EPT, false>(P, st, S, blk, s_c, s_cm, jq, nj - jq, kglob + j0 + jq, s_lum, s_alive, bin,
                                  to_flush, spb, sg.n_steps - (j0 + jq));
     }
   }
@@ -445,7 +513,9 @@ __device__ __forceinline__ void segment_f32(const KParams& P, const mcl_set& st,
 // ---------------------------------------------------------------------------
 // FP32 / Philox kernel
 // ---------------------------------------------------------------------------
-template <int BLOCK, int EPT>
+// FILLS = false builds the kernel without the filling path (fewer
+// registers, more resident warps) for batches whose segments never fill.
+template <int BLOCK, int EPT, bool FILLS>
 __device__ __forceinline__ void kb_f32_body(const KParams& P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const mcl_b_args& a = P.a;
@@ -454,6 +524,7 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
   uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
   uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
   __shared__ int s_item;
+  __shared__ float s_bm[2 * kBlocksPerChunk];
 
   Header* hdr = reinterpret_cast<Header*>(a.workspace);
   const float2* table = reinterpret_cast<const float2*>(reinterpret_cast<const char*>(a.workspace) + kHeaderBytes);
@@ -493,10 +564,15 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
     const float2* tab = table + st.step_offset;
     for (int g = 0; g < st.seg_count; ++g) {
       const mcl_segment sg = a.segs[st.seg_begin + g];
-      if (sg.fill_rate > 0.0)
-        segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
-      else
-        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_lum, s_alive, bbase, kglob, alpha);
+      if (sg.fill_rate > 0.0) {
+        if constexpr (FILLS)
+          segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum, s_alive, bbase, kglob,
+                                        alpha);
+        else  // the caller promised no filling segment (mcl_b_args.no_fill)
+          report(a.status, MCL_EINVAL);
+      } else
+        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum, s_alive, bbase, kglob,
+                                       alpha);
       bbase += (uint32_t)((sg.n_steps + 7) >> 3);
       kglob += sg.n_steps;
     }
@@ -506,15 +582,15 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
   }
 }
 
-template <int BLOCK, int EPT>
+template <int BLOCK, int EPT, bool FILLS>
 __global__ void __launch_bounds__(BLOCK) kb_f32(const KParams P) {
-  kb_f32_body<BLOCK, EPT>(P);
+  kb_f32_body<BLOCK, EPT, FILLS>(P);
 }
 
 // The same kernel compiled for MINB resident CTAs per SM (fewer registers).
-template <int BLOCK, int EPT, int MINB>
+template <int BLOCK, int EPT, int MINB, bool FILLS>
 __global__ void __launch_bounds__(BLOCK, MINB) kb_f32_occ(const KParams P) {
-  kb_f32_body<BLOCK, EPT>(P);
+  kb_f32_body<BLOCK, EPT, FILLS>(P);
 }
 
 // ---------------------------------------------------------------------------
@@ -660,14 +736,14 @@ using KernelFn = void (*)(const KParams);
 
 // Kernel getters, one per translation unit.  `occupancy` 0 selects the
 // default build; another value selects the build compiled for that many
-// resident CTAs per SM (fewer registers), where one exists.  nullptr = no
-// such kernel.
-KernelFn b_f32_128_e2(int occupancy);
-KernelFn b_f32_128_e4(int occupancy);
-KernelFn b_f32_128_e8(int occupancy);
-KernelFn b_f32_256_e2(int occupancy);
-KernelFn b_f32_256_e4(int occupancy);
-KernelFn b_f32_256_e8(int occupancy);
+// resident CTAs per SM (fewer registers), where one exists.  `fills` false
+// selects the build without the filling path.  nullptr = no such kernel.
+KernelFn b_f32_128_e2(int occupancy, bool fills);
+KernelFn b_f32_128_e4(int occupancy, bool fills);
+KernelFn b_f32_128_e8(int occupancy, bool fills);
+KernelFn b_f32_256_e2(int occupancy, bool fills);
+KernelFn b_f32_256_e4(int occupancy, bool fills);
+KernelFn b_f32_256_e8(int occupancy, bool fills);
 KernelFn b_pick_f64(int block, int ept, bool injected);
 
 }  // namespace mcl

@@ -1,13 +1,15 @@
 // FP32 Bernoulli kernel, 256 threads per CTA, 8 slots per thread (one
 // translation unit per variant so that the variants compile in parallel).
-// occupancy 0 = the default build; 2 = the build for 2 resident CTAs per SM (at most 128 registers).
+// Builds with and without the filling path; occupancy 0 = the default build; 2 = the build for 2
+// resident CTAs per SM (at most 128 registers).
 #include "kinetics_b_device.cuh"
 
 namespace mcl {
 
-KernelFn b_f32_256_e8(int occupancy) {
-  if (occupancy == 2) return kb_f32_occ<256, 8, 2>;
-  return occupancy == 0 ? kb_f32<256, 8> : nullptr;
+KernelFn b_f32_256_e8(int occupancy, bool fills) {
+  if (occupancy == 2) return fills ? kb_f32_occ<256, 8, 2, true> : kb_f32_occ<256, 8, 2, false>;
+  if (occupancy == 0) return fills ? kb_f32<256, 8, true> : kb_f32<256, 8, false>;
+  return nullptr;
 }
 
 }  // namespace mcl

@@ -196,3 +196,37 @@ def test_fill_fade_irsl_sequence_fp32_fates():
 def test_fp32_unknown_register_capped_build_is_rejected():
     with pytest.raises(Exception, match="invalid argument|EINVAL|MCL_EINVAL"):
         simulate_batch(mixed_specs()[:2], precision="fp32", seed=5, block=256, ept=8, occupancy=3)
+
+
+@pytest.mark.parametrize("block,ept", [(128, 8), (256, 4)])
+def test_no_fill_build_matches_general_build(block, ept):
+    """Batches that never fill run the build without the filling path; it
+    gives the same bins and fates as the general build."""
+    import torch
+    specs = [s for s in mixed_specs() if all(g.fill_rate == 0 for g in s.segments)]
+    lean = BernoulliBatch(specs, precision="fp32", seed=41, block=block, ept=ept, want_fates=True)
+    full = BernoulliBatch(specs, precision="fp32", seed=41, block=block, ept=ept, want_fates=True)
+    assert lean.no_fill == 1
+    full.args.no_fill = 0
+    lean.launch()
+    full.launch()
+    torch.cuda.synchronize()
+    a, b = lean.result(), full.result()
+    assert lean.status() == 0 and full.status() == 0
+    assert np.array_equal(a.lum, b.lum)
+    assert np.array_equal(a.alive, b.alive)
+    assert np.array_equal(a.fates, b.fates)
+
+
+def test_no_fill_build_reports_a_filling_segment():
+    """A launch that promises no filling segment but has one reports
+    MCL_EINVAL in its status word."""
+    import torch
+    from mcluminescence_gb300 import _lib
+    specs = [s for s in mixed_specs() if any(g.fill_rate > 0 for g in s.segments)]
+    b = BernoulliBatch(specs, precision="fp32", seed=3, block=256, ept=4)
+    assert b.no_fill == 0
+    b.args.no_fill = 1
+    b.launch()
+    torch.cuda.synchronize()
+    assert b.status() == _lib.MCL_EINVAL
