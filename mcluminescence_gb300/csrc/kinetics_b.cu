@@ -21,18 +21,21 @@
 //   parameter bank, so the rounds cost only the multiplies and 3-input XORs;
 // * the CTA copies 256-step chunks of (c_j, q_j) into shared memory;
 // * FP32 mode spends 16 random bits per electron-step in the common case: a
-//   Philox block (four 32-bit words) covers 8 steps of a slot.  The step's
-//   16-bit field h becomes the float 2^23 + h with one byte permute, and one
-//   FFMA gives d = 2^23 + h - c16 w (c16 = c 2^16 from the step table);
-//   d >= 2^23 + 1 proves u >= p, so nothing happens.  Each step keeps the
-//   minimum d over the thread's slots (3-input min).  In segments without
-//   filling one branch per 8-step block enters the exact test, which checks
-//   u32 < ceil(p 2^32), p = -expm1f(-c w), drawing the uniform's low 16 bits
-//   from a separate Philox counter only when h sits on the threshold's upper
-//   half; it runs with probability ~ c w + 2^-16 per trial.  Filling segments branch once per step (a refill
-//   changes the next step's test).  Per trial the fast path is one byte
-//   permute, one FFMA and half a min, next to 1/8 of a Philox call (20
-//   32x32->64 multiplies on the FMA-heavy pipe, 20 3-input XORs);
+//   Philox block (four 32-bit words) covers 8 steps of a slot.  Per 8-step
+//   block the CTA stores the bound cm = RU(max c16 (1 + 2^-20)) (c16 = c 2^16
+//   from the step table); per slot one FFMA turns cm w into an integer
+//   threshold TI > h of every trial that can escape, and each word tests its
+//   two 16-bit fields against TI with one subtraction and one LOP3 (filling
+//   segments use the refill bound for empty traps).  A slot with no flagged
+//   field has no event in the block; a flagged one is drawn again out of
+//   line and tested step by step: the float test d = 2^23 + h - c16 w <
+//   2^23 + 1, then the exact test u32 < ceil(p 2^32), p = -expm1f(-c w),
+//   drawing the uniform's low 16 bits from a separate Philox counter only
+//   when h sits on the threshold's upper half.  Per trial the fast path is
+//   about one instruction next to 1/8 of a Philox call (17 32x32->64
+//   multiplies per block on the FMA-heavy pipe, 20 3-input XORs);
+// * batches without filling segments (mcl_b_args.no_fill) run a build
+//   without the filling path: fewer registers, more resident warps;
 // * events are added to shared-memory bins (rare); at each bin end the warp
 //   sums the filled-trap counts with one reduction; when an item ends the CTA
 //   adds every non-zero bin to HBM with one atomic.
