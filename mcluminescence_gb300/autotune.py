@@ -24,13 +24,18 @@ CANDIDATES = {
 CACHE = os.path.join(_build.LIBDIR, "autotune.json")
 
 
+def _no_fill(specs: Sequence[SetSpec]) -> bool:
+    return all(g.fill_rate <= 0.0 for s in specs for g in s.segments)
+
+
 def _bucket(specs: Sequence[SetSpec], precision: str) -> str:
     import torch
     mb = max(s.n_bins for s in specs)
     steps = sum(s.total_steps for s in specs) / max(len(specs), 1)
     slots = sum(s.n_slots for s in specs) / max(len(specs), 1)
     return (f"{torch.cuda.get_device_name()}|{precision}|bins{2 ** math.ceil(math.log2(max(mb, 1)))}"
-            f"|steps{2 ** round(math.log2(max(steps, 1)))}|slots{2 ** round(math.log2(max(slots, 1)))}")
+            f"|steps{2 ** round(math.log2(max(steps, 1)))}|slots{2 ** round(math.log2(max(slots, 1)))}"
+            f"|{'nofill' if _no_fill(specs) else 'fill'}")
 
 
 def _load():
@@ -41,7 +46,7 @@ def _load():
         return {}
 
 
-def time_shape(specs, precision, block, ept, occupancy=0, reps=2) -> float:
+def time_shape(specs, precision, block, ept, occupancy=0, reps=4) -> float:
     import torch
     from .batch import BernoulliBatch
     b = BernoulliBatch(specs, precision=precision, seed=1, block=block, ept=ept, want_alive=True,
@@ -66,8 +71,13 @@ def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
     if key in cache and len(cache[key]["best"]) == 3:
         return tuple(cache[key]["best"])
     sample = list(specs[::32]) or list(specs)
+    cands = CANDIDATES[precision]
+    if _no_fill(specs):
+        # the builds without the filling path already use 54-80 registers: the
+        # register-capped builds only matter when the filling path is compiled in
+        cands = [c for c in cands if c[2] == 0]
     times = {}
-    for blk, ept, occ in CANDIDATES[precision]:
+    for blk, ept, occ in cands:
         times[(blk, ept, occ)] = time_shape(sample, precision, blk, ept, occ)
     best = min(times, key=times.get)
     cache = _load()
