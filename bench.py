@@ -271,7 +271,8 @@ def main():
                                "(150-300 C, 1e4 s, dt 1 s)",
                    "sets_per_gpu": a.sets, "traps_per_gpu": int(sum(s.n_slots for s in specs)),
                    "trials_per_step_per_gpu": int(trials), "precision": "fp32",
-                   "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ, "n_items": batch.n_items,
+                   "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ,
+                   "filling_path_built": not batch.no_fill, "n_items": batch.n_items,
                    "l2": "flushed between passes (256 MB write, untimed)",
                    "parallelism": f"replicas x{world} (independent sets, no collective)"},
         # each replayed pass launches the rate-table pre-pass and the kinetics kernel
@@ -359,7 +360,7 @@ def sequence_bench(a, rank):
     ms = e0.elapsed_time(e1) / reps
     steps = [s.total_steps for s in specs]
     return {"sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": ms,
-            "block": block, "ept": ept, "occupancy_build": occ,
+            "block": block, "ept": ept, "occupancy_build": occ, "filling_path_built": not b.no_fill,
             "electron_steps_per_s": b.trials / (ms / 1e3), "steps_min": min(steps), "steps_max": max(steps),
             "events_per_pass": int(b.result().lum.sum())}
 

@@ -170,7 +170,8 @@ __device__ __forceinline__ uint32_t field16(uint32_t word) {
   return (T < 4) ? (word >> 16) : (word & 0xffffu);
 }
 
-// Fast test of the FP32 mode.  The shared-memory step table holds
+// Per-step float test of the FP32 mode (run for the traps the integer
+// prefilter below flags).  The shared-memory step table holds
 // c16 = c * 2^16 and q16 = q * 2^16 (exact power-of-two scalings).  For a
 // filled trap d = fl(2^23 + h - c16 w) (one FFMA), for an empty trap of a
 // filling segment d = fl(2^23 + h - q16).  An event needs u32 < ceil(p 2^32)
@@ -182,22 +183,6 @@ __device__ __forceinline__ uint32_t field16(uint32_t word) {
 // trials, which go to the exact test.
 constexpr float kCand = 8388609.0f;  // 2^23 + 1
 constexpr float kInv16 = 0x1p-16f;
-
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-  float d;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-  return d;
-}
-
-template <int N>
-__device__ __forceinline__ float min_all(const float (&d)[N]) {
-  float m = d[0];
-  int i = 1;
-#pragma unroll
-  for (; i + 1 < N; i += 2) m = min3f(m, d[i], d[i + 1]);
-  if (i < N) m = fminf(m, d[i]);
-  return m;
-}
 
 // Per-thread state of the FP32 kernel for one work item.
 template <int EPT>
