@@ -86,10 +86,12 @@ def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
     best = min(times, key=times.get)
     cache = _load()
     cache[key] = {"best": list(best), "ms": {f"{b}x{e}/{o}": t for (b, e, o), t in times.items()}}
-    try:
+    try:  # write-then-rename: processes sharing the library never see a torn file
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-        with open(CACHE, "w") as f:
+        tmp = f"{CACHE}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
             json.dump(cache, f, indent=1)
+        os.replace(tmp, CACHE)
     except OSError:
         pass
     return best
