@@ -20,7 +20,7 @@ bit-exact with the reference when both consume the same uniform stream
 * waits: legacy ``exponential(scale) = scale * -log(1 - U)`` with the C
   library ``log`` (numpy's vectorised ``log`` differs in the last bit)
                                      src/class/tl_trap_lab.py:48-60
-* the driver loop and output tables  src/class/simulate.py:36-92
+* the simulation loop and output tables  src/class/simulate.py:36-92
 
 Instead of the reference's dense electron x hole distance matrix (whose
 ``np.delete`` costs 94 % of its run time) the oracle keeps per electron the
