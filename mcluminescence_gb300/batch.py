@@ -200,6 +200,10 @@ class BernoulliBatch:
         torch = _torch()
         s = stream if stream is not None else torch.cuda.Stream()
         self._graph_stream = s
+        if self._graph is not None:  # re-capture: release the previous graph
+            torch.cuda.synchronize()  # after its replays have finished
+            self.lib.mcl_graph_destroy(self._graph)
+            self._graph = None
         g = C.c_void_p()
         _lib.check(self.lib.mcl_b_graph_create(C.byref(self.args), C.c_void_p(int(s.cuda_stream)),
                                                C.byref(g)), "mcl_b_graph_create")

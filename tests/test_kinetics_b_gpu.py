@@ -95,6 +95,21 @@ def test_fp32_launch_shape_invariance(block, ept, occ):
     assert np.array_equal(ref.fates, got.fates)
 
 
+def test_recapture_replaces_the_graph():
+    import torch
+    specs = mixed_specs()[:3]
+    b = BernoulliBatch(specs, precision="fp32", seed=17)
+    s = torch.cuda.Stream()
+    b.capture(s)
+    b.replay(s)
+    s.synchronize()
+    first = b.result().lum.copy()
+    b.capture(s)
+    b.replay(s)
+    s.synchronize()
+    assert np.array_equal(b.result().lum, first)
+
+
 def test_graph_replay_is_deterministic():
     import torch
     specs = mixed_specs()
