@@ -10,10 +10,11 @@ Two denominators are reported:
 * ``issue``: the algorithmic operation count per electron-step trial -- one
   eighth of a Philox4x32-10 block (10 rounds of two 32x32->64 multiplies and
   two 3-input XORs = 40 operations per block of 8 trials = 5) plus three
-  for the fast test (one byte permute forms 2^23 + h from the 16-bit field,
-  one FFMA forms d, half a 3-input min keeps the step's minimum; counted as
-  3) = 8 -- against the issue peak of 4 sub-partitions x 32 lanes x SM clock
-  x SMs.  The ALU pipe (XORs, permutes, mins) issues at half that rate and
+  for the Bernoulli test itself (scale, compare, select) = 8, a fixed count
+  of the algorithm's work (the kernel's integer prefilter spends about one
+  instruction per trial on the test) -- against the issue peak of 4
+  sub-partitions x 32 lanes x SM clock x SMs.  The ALU pipe (XORs, the
+  prefilter's subtractions and LOP3s) issues at half that rate and
   a 32x32->64 multiply takes about four FMA-heavy cycles per warp, so this
   peak is above what any Philox4x32-10 kernel reaches;
 * ``philox``: the measured rate of a kernel that only generates Philox blocks
