@@ -71,3 +71,16 @@ def test_event_workspace_layout_matches_validation(n_e, holes):
         if i + 1 < len(sims):
             assert end <= offs[i + 1]
     assert (n_e <= 2000) == bool(smem.value)
+
+
+def test_batches_without_filling_are_recognised():
+    """The autotuner and the packer both key the lean (no filling path) build
+    on every segment having fill_rate == 0."""
+    from mcluminescence_gb300 import autotune, schedule
+    from mcluminescence_gb300.batch import pack_host
+    tl = schedule.batch_tl_iso(64, seed=1)
+    dose = schedule.batch_dose_fade_irsl(16, seed=1)
+    assert autotune._no_fill(tl) and not autotune._no_fill(dose)
+    assert not (pack_host(tl)[1]["fill_rate"] > 0).any()
+    assert (pack_host(dose)[1]["fill_rate"] > 0).any()
+    assert all(c[2] == 0 or c[1] in (2, 4, 8) for c in autotune.CANDIDATES["fp32"])
