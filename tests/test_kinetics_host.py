@@ -83,4 +83,3 @@ def test_batches_without_filling_are_recognised():
     assert autotune._no_fill(tl) and not autotune._no_fill(dose)
     assert not (pack_host(tl)[1]["fill_rate"] > 0).any()
     assert (pack_host(dose)[1]["fill_rate"] > 0).any()
-    assert all(c[2] == 0 or c[1] in (2, 4, 8) for c in autotune.CANDIDATES["fp32"])
