@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MCL_ABI_VERSION 1
+#define MCL_ABI_VERSION 2
 
 /* ---- return / status codes ------------------------------------------- */
 #define MCL_OK 0
@@ -103,7 +103,14 @@ typedef struct mcl_item {
   int32_t slot_begin;
 } mcl_item;
 
-/* Arguments of one Bernoulli launch (all pointers are device pointers). */
+/* Arguments of one Bernoulli launch (all pointers are device pointers).
+ * The kernels check every set against the sizes declared here before they
+ * touch a buffer: segments within n_segs, the set's steps (the sum of its
+ * segments' n_steps) within table_steps from step_offset, bins within
+ * n_bins_total and max_bins, slots within n_slots_total, injected uniforms
+ * within n_uniforms, and every item's set and first slot.  A set or item
+ * that fails writes MCL_ECAPACITY (MCL_EINVAL for a bad item) to the status
+ * word and is skipped: nothing is read or written outside the buffers. */
 typedef struct mcl_b_args {
   const mcl_set* sets;
   const mcl_segment* segs;
@@ -118,6 +125,7 @@ typedef struct mcl_b_args {
   int64_t table_steps;     /* sum of total_steps over all sets (table rows)    */
   int64_t n_bins_total;
   int64_t n_slots_total;
+  int64_t n_uniforms;      /* injected mode: elements of uniforms[]            */
   uint64_t seed;
   int32_t n_sets;
   int32_t n_segs;

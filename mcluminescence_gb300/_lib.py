@@ -23,6 +23,8 @@ MCL_ENODEV = -5
 MCL_ENOHOLE = -6
 MCL_EOVERFLOW = -7
 
+ABI_VERSION = 2
+
 MCL_FP32 = 0
 MCL_FP64 = 1
 MCL_RNG_PHILOX = 0
@@ -48,7 +50,8 @@ class BArgs(C.Structure):
         ("sets", C.c_void_p), ("segs", C.c_void_p), ("items", C.c_void_p),
         ("lum", C.c_void_p), ("alive", C.c_void_p), ("fates", C.c_void_p),
         ("uniforms", C.c_void_p), ("status", C.c_void_p), ("workspace", C.c_void_p),
-        ("workspace_bytes", C.c_int64), ("table_steps", C.c_int64), ("n_bins_total", C.c_int64), ("n_slots_total", C.c_int64), ("seed", C.c_uint64),
+        ("workspace_bytes", C.c_int64), ("table_steps", C.c_int64), ("n_bins_total", C.c_int64),
+        ("n_slots_total", C.c_int64), ("n_uniforms", C.c_int64), ("seed", C.c_uint64),
         ("n_sets", C.c_int32), ("n_segs", C.c_int32), ("n_items", C.c_int32),
         ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
         ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
@@ -90,11 +93,16 @@ class AdamTensor(C.Structure):
 
 
 class MclError(RuntimeError):
-    def __init__(self, code: int, what: str):
+    """A negative status.  ``detail`` appends the library's last error text
+    (set by the entry point that just returned ``code``); device status words
+    pass ``detail=False``, as no entry point set a text for them."""
+
+    def __init__(self, code: int, what: str, detail: bool = True):
         self.code = code
         lib = _LIB[0]
         msg = lib.mcl_status_string(code).decode() if lib is not None else str(code)
-        extra = lib.mcl_last_error().decode() if (lib is not None and code == MCL_ECUDA) else ""
+        extra = (lib.mcl_last_error().decode()
+                 if (detail and lib is not None and code in (MCL_ECUDA, MCL_ECAPACITY)) else "")
         super().__init__(f"{what}: {msg}" + (f" ({extra})" if extra else ""))
 
 
@@ -173,7 +181,7 @@ def load(auto_build: bool = False):
                 f"CUDA library {path} is not built; run `python -c \"import __graft_entry__ as g; "
                 f"g.build()\"` or `python -m mcluminescence_gb300.build` (there is no CPU fallback)")
         lib = _declare(C.CDLL(path))
-        if lib.mcl_abi_version() != 1:
+        if lib.mcl_abi_version() != ABI_VERSION:
             raise RuntimeError("libmclum ABI version mismatch; rebuild the library")
         sizes = (C.c_size_t * 6)()
         lib.mcl_struct_sizes(sizes)

@@ -160,6 +160,7 @@ class BernoulliBatch:
                         if want_fates else None)
         self.d_u = (torch.from_numpy(np.ascontiguousarray(uniforms[:n_u], dtype=np.float64)).to(dev)
                     if self.rng == _lib.MCL_RNG_INJECTED else None)
+        self.n_uniforms = n_u
         self.d_status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.table_steps = int(np.sum(sets["total_steps"]))
         self.ws_bytes = int(self.lib.mcl_b_workspace_size(_lib.ptr(sets), len(sets), self.precision))
@@ -177,6 +178,7 @@ class BernoulliBatch:
         a.status, a.workspace = _lib.ptr(self.d_status), _lib.ptr(self.d_ws)
         a.workspace_bytes, a.table_steps = self.ws_bytes, self.table_steps
         a.n_bins_total, a.n_slots_total, a.seed = self.n_bins_total, self.n_slots_total, self.seed
+        a.n_uniforms = self.n_uniforms
         a.n_sets, a.n_segs, a.n_items = len(self.host_sets), len(self.host_segs), self.n_items
         a.slots_per_item, a.max_bins = self.block * self.ept, self.max_bins
         a.precision, a.rng, a.block, a.ept, a.grid = self.precision, self.rng, self.block, self.ept, self.grid
@@ -230,7 +232,7 @@ class BernoulliBatch:
     def result(self) -> BatchResult:
         st = self.status()
         if st != 0:
-            raise _lib.MclError(st, "kinetics kernel reported")
+            raise _lib.MclError(st, "kinetics kernel reported", detail=False)
         lum = self.d_lum.cpu().numpy().view(np.uint32)[:self.n_bins_total]
         alive = self.d_alive.cpu().numpy().view(np.uint32)[:self.n_bins_total] if self.d_alive is not None else None
         fates = self.d_fates.cpu().numpy()[:self.n_slots_total] if self.d_fates is not None else None

@@ -21,6 +21,10 @@ extern "C" void mcl_set_last_cuda_error(cudaError_t e) {
   std::snprintf(g_last_msg, sizeof(g_last_msg), "CUDA error %d: %s", (int)e, cudaGetErrorString(e));
 }
 
+extern "C" void mcl_set_last_message(const char* msg) {
+  std::snprintf(g_last_msg, sizeof(g_last_msg), "%s", msg ? msg : "");
+}
+
 extern "C" int mcl_abi_version(void) { return MCL_ABI_VERSION; }
 
 extern "C" const char* mcl_last_error(void) { return g_last_msg; }

@@ -65,3 +65,5 @@ __device__ __forceinline__ void report(int32_t* status, int32_t code) {
   } while (0)
 
 extern "C" void mcl_set_last_cuda_error(cudaError_t e);
+// Sets the text mcl_last_error() returns on this thread.
+extern "C" void mcl_set_last_message(const char* msg);

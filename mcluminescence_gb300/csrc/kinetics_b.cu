@@ -91,7 +91,7 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
       a.workspace_bytes < (int64_t)kHeaderBytes + a.table_steps * (int64_t)table_entry_bytes(a.precision))
     return MCL_ECAPACITY;
   if (a.slots_per_item != a.block * a.ept) return MCL_EINVAL;
-  if (a.rng == MCL_RNG_INJECTED && !a.uniforms) return MCL_EINVAL;
+  if (a.rng == MCL_RNG_INJECTED && (!a.uniforms || a.n_uniforms < 0)) return MCL_EINVAL;
   KernelFn fn = pick_kernel(a);
   if (!fn) return MCL_EINVAL;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

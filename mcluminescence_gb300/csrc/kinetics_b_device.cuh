@@ -64,12 +64,63 @@ __device__ __forceinline__ void step_constants(const mcl_set& st, const mcl_segm
   q = sg.fill_rate > 0.0 ? -expm1(__dmul_rn(-dtj, sg.fill_rate)) : 0.0;
 }
 
-// Pre-pass: one CTA per set fills its rows of the (c_j, q_j) table.
+// Extents of set st against the sizes the launch declares (a C caller may
+// pass sets whose offsets disagree with them).  Returns the set's step count
+// (the sum of its segments' n_steps, which is what the kernels index with),
+// or -1 if a segment, table row, bin, slot or injected uniform of the set
+// would fall outside its buffer.  Every thread of a CTA evaluates it for the
+// same set, so the answer is uniform over the CTA.
+__device__ __forceinline__ int64_t checked_steps(const mcl_b_args& a, const mcl_set& st) {
+  if (st.seg_begin < 0 || st.seg_count < 0 || (int64_t)st.seg_begin + st.seg_count > a.n_segs) return -1;
+  if (st.n_slots < 0 || st.n_filled < 0 || st.n_filled > st.n_slots) return -1;
+  if (st.n_bins < 0 || st.n_bins > a.max_bins || st.bin_offset < 0 || st.bin_offset + st.n_bins > a.n_bins_total)
+    return -1;
+  if (st.slot_offset < 0 || st.slot_offset + st.n_slots > a.n_slots_total) return -1;
+  int64_t steps = 0;
+  for (int g = 0; g < st.seg_count; ++g) {
+    const mcl_segment& sg = a.segs[st.seg_begin + g];
+    if (sg.n_steps < 0 || sg.steps_per_bin < 1 || sg.bin_offset < 0) return -1;
+    if ((int64_t)sg.bin_offset + ((int64_t)sg.n_steps + sg.steps_per_bin - 1) / sg.steps_per_bin > st.n_bins)
+      return -1;
+    steps += sg.n_steps;
+  }
+  if (steps > 0x7fffffff || st.step_offset < 0 || st.step_offset + steps > a.table_steps) return -1;
+  if (a.rng == MCL_RNG_INJECTED &&
+      (st.u_offset < 0 || st.u_offset + (int64_t)st.n_slots * (1 + steps) > a.n_uniforms))
+    return -1;
+  return steps;
+}
+
+// The item's set, or -1 (with the status word set) if the item or its set
+// fails the extent checks.
+__device__ __forceinline__ int checked_item(const mcl_b_args& a, const mcl_item& item) {
+  if (item.set < 0 || item.set >= a.n_sets) {
+    report(a.status, MCL_EINVAL);
+    return -1;
+  }
+  const mcl_set& st = a.sets[item.set];
+  if (item.slot_begin < 0 || item.slot_begin >= st.n_slots) {
+    report(a.status, MCL_EINVAL);
+    return -1;
+  }
+  if (checked_steps(a, st) < 0) {
+    report(a.status, MCL_ECAPACITY);
+    return -1;
+  }
+  return item.set;
+}
+
+// Pre-pass: one CTA per set fills its rows of the (c_j, q_j) table (none if
+// the set's rows would leave the table).
 template <typename T>
 __global__ void __launch_bounds__(256) kb_tables(const mcl_b_args a) {
   const int s = blockIdx.x;
   if (s >= a.n_sets) return;
   const mcl_set st = a.sets[s];
+  if (checked_steps(a, st) < 0) {
+    if (threadIdx.x == 0) report(a.status, MCL_ECAPACITY);
+    return;
+  }
   T* tab = reinterpret_cast<T*>(reinterpret_cast<char*>(a.workspace) + kHeaderBytes) + 2 * st.step_offset;
   int64_t base = 0;
   for (int g = 0; g < st.seg_count; ++g) {
@@ -521,12 +572,11 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
     const int it = s_item;
     if (it >= a.n_items) break;
     const mcl_item item = a.items[it];
-    const mcl_set st = a.sets[item.set];
-    if (st.n_bins > a.max_bins) {  // host validation makes this unreachable
-      report(a.status, MCL_ECAPACITY);
+    if (checked_item(a, item) < 0) {  // host validation makes this unreachable
       __syncthreads();
       continue;
     }
+    const mcl_set st = a.sets[item.set];
     zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
 
     const float alpha = (float)st.alpha;
@@ -601,12 +651,11 @@ __global__ void __launch_bounds__(BLOCK) kb_f64(const KParams P) {
     const int it = s_item;
     if (it >= a.n_items) break;
     const mcl_item item = a.items[it];
-    const mcl_set st = a.sets[item.set];
-    if (st.n_bins > a.max_bins) {
-      report(a.status, MCL_ECAPACITY);
+    if (checked_item(a, item) < 0) {
       __syncthreads();
       continue;
     }
+    const mcl_set st = a.sets[item.set];
     zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
 
     double w[EPT];

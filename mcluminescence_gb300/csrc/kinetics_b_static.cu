@@ -20,7 +20,15 @@
 // The ticket is cleared and the whole table rewritten by every call, so no
 // stale state leaks between calls; but two calls whose work overlaps on the
 // GPU (different streams, or different host threads) race on the array and
-// corrupt each other's results -- serialise them on one stream.
+// corrupt each other's results -- serialise them on one stream.  The kernels
+// check every set's table rows against table_steps (which is checked against
+// the array's size here), so sets that disagree with the declared sizes are
+// refused on the device instead of writing past the array.
+//
+// The array's device address is looked up once per device and kept for the
+// life of the process: a device reset (cudaDeviceReset) after the first call
+// on that device is not supported, as the cached address would then be
+// stale.
 #include <cstdio>
 #include <mutex>
 
@@ -34,8 +42,6 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
 
-thread_local char g_static_msg[256] = "";
-
 }  // namespace
 
 extern "C" int mcl_b_run_static(const mcl_b_args* args, void* stream) {
@@ -43,11 +49,12 @@ extern "C" int mcl_b_run_static(const mcl_b_args* args, void* stream) {
   const int64_t entry = args->precision == MCL_FP64 ? 16 : 8;
   const int64_t capacity = ((int64_t)MCL_B_STATIC_SCRATCH_BYTES - 256) / entry;
   if (args->table_steps < 0 || args->table_steps > capacity) {
-    std::snprintf(g_static_msg, sizeof(g_static_msg),
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
                   "mcl_b_run_static: the batch has %lld steps over all sets; the static "
                   "scratch of %d bytes holds at most %lld in this precision",
                   (long long)args->table_steps, (int)MCL_B_STATIC_SCRATCH_BYTES, (long long)capacity);
-    std::fprintf(stderr, "%s\n", g_static_msg);
+    mcl_set_last_message(msg);
     return MCL_ECAPACITY;
   }
   // Set-up, once per device, with that device current: the host-side name of

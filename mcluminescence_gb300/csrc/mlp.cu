@@ -422,6 +422,7 @@ __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __n
   const uint32_t tmem = tmem_slot;
   constexpr uint32_t idesc = idesc_bf16(kM, NT);
   bool ok = true;
+  int last_commit = -1;  // the last slab whose MMAs were committed (uniform over the CTA)
   for (int it = 0; it < nk; ++it) {
     const int q = it % kStages;
     cp_async_wait_1();  // this thread's copies of slab it have landed
@@ -438,6 +439,7 @@ __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __n
       }
       commit(mb0 + 8 * q);
     }
+    last_commit = it;
     __syncwarp();
     if (it + 2 < nk) {
       // slab it + 2 reuses the buffer of slab it - 1: wait for that MMA first
@@ -451,8 +453,12 @@ __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __n
     }
     cp_async_commit();
   }
-  if (ok) {  // the last commit covers every MMA before it
-    const int j = nk - 1;
+  // Whatever happened above, no MMA may still write tensor memory when it is
+  // read or freed: wait for the last commit issued, which covers every MMA
+  // before it.  After an earlier timeout this is the second, again bounded,
+  // wait; the kernel then frees its tensor memory either way.
+  if (last_commit >= 0) {
+    const int j = last_commit;
     if (!mbar_wait(mb0 + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u)) ok = false;
   }
   asm volatile("cp.async.wait_all;" ::: "memory");

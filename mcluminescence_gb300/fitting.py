@@ -48,7 +48,7 @@ def mc_curves(params: np.ndarray, n_traps: int, seed: int, id0: int = 0):
     b.launch()
     st = b.status()
     if st:
-        raise _lib.MclError(st, "kinetics kernel reported")
+        raise _lib.MclError(st, "kinetics kernel reported", detail=False)
     return b.d_lum[:len(params) * S.N_BINS].view(len(params), S.N_BINS).float()
 
 

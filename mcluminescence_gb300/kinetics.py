@@ -274,7 +274,7 @@ def _raise_for(status: np.ndarray, steps: int):
         if code == _lib.MCL_ENOHOLE:
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
         if code != _lib.MCL_OK:
-            raise _lib.MclError(code, "event-driven kinetics kernel")
+            raise _lib.MclError(code, "event-driven kinetics kernel", detail=False)
 
 
 def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,

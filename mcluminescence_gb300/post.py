@@ -120,7 +120,7 @@ def tl_glow_curves(x_ax, lum, T_start: Sequence[float], T_rate: Sequence[float],
                "mcl_glow_hist")
     st = int(d_status.item())
     if st != 0:
-        raise _lib.MclError(st, "mcl_glow_hist (lum entries must be 0/1 event flags)")
+        raise _lib.MclError(st, "mcl_glow_hist (lum entries must be 0/1 event flags)", detail=False)
     k = max(1, int(win_deg / bin_width))
     return running_mean_offsets(d_hist, b_off, k)
 

@@ -225,29 +225,64 @@ def injected_size(st: dict) -> int:
     return int(st["n_slots"]) * (1 + total_steps(st))
 
 
-def expected_lum(st: dict, n_u: int = 200000) -> np.ndarray:
-    """Expected recombinations per bin (FP64, no sampling) for a set without
-    filling: P(event in bin) = E_r'[S(k0) - S(k1)] with survival
-    S(k) = exp(-w(r') * sum_{j<k} c_j), averaged over r' by the midpoint rule
-    in the uniform variable of the inverse CDF."""
-    if any(float(s.get("fill_rate", 0.0)) > 0 for s in st["segments"]):
-        raise ValueError("expected_lum covers schedules without filling")
+def expected_curves(st: dict, n_u: int = 200000):
+    """Expected recombinations per bin and expected filled traps at each bin
+    end (FP64, no sampling); returns ``(lum, alive)``.
+
+    Every trap is an independent two-state chain (filled with some w, or
+    empty), so expectations obey a linear recursion.  The w of a filled trap
+    is carried on a quadrature grid: w_i = exp(-alpha r'(u_i)) at the
+    midpoints u_i of n_u equal cells of the inverse-CDF variable, each node
+    holding the expected number of filled traps with that w.  In a segment
+    without filling a filled trap survives to local step k with probability
+    exp(-w sum_{j<k} c_j), so each bin's expected escapes follow in closed
+    form; in a filling segment the chain is stepped: per step a filled trap
+    escapes with p_j(w) = 1 - exp(-c_j w) and an empty one refills with q_j,
+    drawing a fresh w from the same distribution (equal weight per node).  A
+    trap that escapes in a step is not refilled in it, as in ``run_set``."""
     u = (np.arange(n_u) + 0.5) / n_u
     w = np.exp(-float(st["alpha"]) * _r_prime(u))
+    n = int(st["n_slots"])
+    n_filled = int(st["n_filled"])
+    f = np.full(n_u, n_filled / n_u)      # expected filled traps per node
+    e = float(n - n_filled)               # expected empty traps
     n_bins = int(st["n_bins"])
-    out = np.zeros(n_bins)
-    C = 0.0
-    S_prev = np.ones_like(w)
+    lum = np.zeros(n_bins)
+    alive = np.zeros(n_bins)
     for seg in st["segments"]:
-        c, _ = segment_constants(st, seg)
-        cum = np.cumsum(c)
+        c, q = segment_constants(st, seg)
         spb = int(seg["steps_per_bin"])
         b0 = int(seg["bin_offset"])
-        n = int(seg["n_steps"])
-        for b in range((n + spb - 1) // spb):
-            end = min((b + 1) * spb, n) - 1
-            S = np.exp(-w * (C + cum[end]))
-            out[b0 + b] += np.mean(S_prev - S)
-            S_prev = S
-        C += cum[-1] if n else 0.0
-    return out * int(st["n_filled"])
+        ns = int(seg["n_steps"])
+        if ns == 0:
+            continue
+        if float(seg.get("fill_rate", 0.0)) > 0:
+            for j in range(ns):
+                esc = f * -np.expm1(-c[j] * w)
+                E = float(esc.sum())
+                refill = e * q[j]
+                f = f - esc + refill / n_u
+                e = e - refill + E
+                lum[b0 + j // spb] += E
+                if (j + 1) % spb == 0 or j + 1 == ns:
+                    alive[b0 + j // spb] = float(f.sum())
+            continue
+        cum = np.cumsum(c)
+        C_prev = 0.0
+        S_prev = np.ones_like(w)
+        for b in range((ns + spb - 1) // spb):
+            C = cum[min((b + 1) * spb, ns) - 1]
+            # S_prev - S without cancellation: S_prev * (1 - exp(-w (C - C_prev)))
+            d = S_prev * -np.expm1(-w * (C - C_prev))
+            lum[b0 + b] = float(np.dot(f, d))
+            S_prev = S_prev - d
+            C_prev = C
+            alive[b0 + b] = float(np.dot(f, S_prev))
+        e += float(np.dot(f, 1.0 - S_prev))
+        f = f * S_prev
+    return lum, alive
+
+
+def expected_lum(st: dict, n_u: int = 200000) -> np.ndarray:
+    """Expected recombinations per bin (``expected_curves``' first output)."""
+    return expected_curves(st, n_u)[0]

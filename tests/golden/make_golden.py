@@ -1,9 +1,9 @@
 """Generate the golden fixtures by running the UNMODIFIED reference.
 
-Run in a container that has the reference checkout (default path below, or
-``MCL_REFERENCE``)::
+Run where the reference checkout is available, with ``MCL_REFERENCE``
+naming its root::
 
-    python tests/golden/make_golden.py            # writes tests/golden/kinetics_k.npz
+    MCL_REFERENCE=<checkout> python tests/golden/make_golden.py   # writes tests/golden/kinetics_k.npz
 
 What it does
 * puts the stand-in ``omegaconf``/``hydra``/``pandas``/``matplotlib`` modules
@@ -33,7 +33,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("MCL_REFERENCE", "/root/reference")
+sys.path.insert(0, HERE)
+from refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 
 sys.path.insert(0, os.path.join(HERE, "refshim"))
 sys.path.insert(0, os.path.join(REF, "src", "class"))

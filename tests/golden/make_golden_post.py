@@ -6,9 +6,9 @@ Runs the UNMODIFIED reference functions ``hist_and_smooth`` / ``running_mean``
 on synthetic inputs and on the tables of the ``tl12_small`` golden case, and
 writes ``tests/golden/post.npz``::
 
-    python tests/golden/make_golden_post.py
+    MCL_REFERENCE=<checkout> python tests/golden/make_golden_post.py
 
-Needs the reference checkout (default below, or ``MCL_REFERENCE``) and the
+Needs the reference checkout (``MCL_REFERENCE`` names its root) and the
 stand-in modules of ``tests/golden/refshim``.
 """
 from __future__ import annotations
@@ -20,7 +20,10 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("MCL_REFERENCE", "/root/reference")
+sys.path.insert(0, HERE)
+from refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 sys.path.insert(0, os.path.join(HERE, "refshim"))
 sys.path.insert(0, os.path.join(REF, "src", "class"))
 

@@ -245,3 +245,60 @@ def test_no_fill_build_reports_a_filling_segment():
     b.launch()
     torch.cuda.synchronize()
     assert b.status() == _lib.MCL_EINVAL
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("what", ["table_steps", "n_bins_total", "n_slots_total", "n_segs", "item_set",
+                                  "item_slot"])
+def test_device_refuses_sets_outside_the_declared_sizes(precision, what):
+    """A C caller whose sets disagree with the sizes it declares in
+    mcl_b_args gets a status code instead of reads and writes past its
+    buffers.  Every buffer here is allocated for the sets' real extents, so a
+    missed check could not leave its allocation."""
+    import ctypes as C
+    import torch
+    from mcluminescence_gb300 import _lib
+    lib = _lib.load()
+    specs = mixed_specs()
+    b = BernoulliBatch(specs, precision=precision, seed=5, want_fates=True)
+    a = b._make_args(zero_outputs=1)
+    want = _lib.MCL_ECAPACITY
+    keep = None
+    if what == "table_steps":      # the last set's rows end one past the table
+        a.table_steps -= 1
+    elif what == "n_bins_total":
+        a.n_bins_total -= 1
+    elif what == "n_slots_total":
+        a.n_slots_total -= 1
+    elif what == "n_segs":
+        a.n_segs -= 1
+    else:
+        items = b.host_items.copy()
+        if what == "item_set":
+            items["set"][0] = len(specs)
+        else:
+            items["slot_begin"][0] = -256
+        keep = torch.from_numpy(items.view(np.uint8)).cuda()
+        a.items = keep.data_ptr()
+        want = _lib.MCL_EINVAL
+    rc = lib.mcl_b_run(C.byref(a), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert b.status() == want
+
+
+def test_device_refuses_too_few_injected_uniforms():
+    import ctypes as C
+    import torch
+    from mcluminescence_gb300 import _lib
+    lib = _lib.load()
+    specs = [s for s in mixed_specs() if all(g.fill_rate == 0 for g in s.segments)]
+    from mcluminescence_gb300.batch import pack_host
+    n_u = int(pack_host(specs)[4][-1])
+    u = np.random.default_rng(3).random(n_u)
+    b = BernoulliBatch(specs, precision="fp64", rng="injected", uniforms=u, seed=0)
+    a = b._make_args(zero_outputs=1)
+    a.n_uniforms -= 1
+    assert lib.mcl_b_run(C.byref(a), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    torch.cuda.synchronize()
+    assert b.status() == _lib.MCL_ECAPACITY

@@ -63,13 +63,42 @@ def test_static_scratch_matches_workspace_launch(precision):
             assert np.array_equal(x, y)
 
 
-def test_static_scratch_rejects_oversized_batch():
-    """Refused on the host, before any device work (no GPU needed)."""
+@pytest.mark.gpu
+def test_static_scratch_refuses_sets_beyond_the_declared_table():
+    """Sets whose rate-table rows run past the declared table_steps are
+    refused on the device (status MCL_ECAPACITY), so they cannot write past
+    the shared array.  The sets' real rows fit the array many times over, so a
+    missed check could not leave it either."""
+    import torch
+    from mcluminescence_gb300 import BernoulliBatch
+    b = BernoulliBatch(_specs(), precision="fp32", seed=3)
+    args = b._make_args(zero_outputs=1)
+    args.table_steps = 100
+    lib = _lib.load()
+    rc = lib.mcl_b_run_static(C.byref(args), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert b.status() == _lib.MCL_ECAPACITY
+
+
+# The static array holds 16 MiB: a 256-byte ticket header, then 8-byte (FP32)
+# or 16-byte (FP64) table rows.
+CAPACITY = {_lib.MCL_FP32: 2_097_120, _lib.MCL_FP64: 1_048_560}
+
+
+def test_static_scratch_capacity_boundary():
+    """Refused on the host one row over the capacity, before any device work;
+    a batch of exactly the capacity passes the host check (it then fails for
+    other reasons here: no outputs, and no GPU on a CPU-only machine).  No GPU
+    needed."""
     lib = _lib.load(auto_build=True)
-    a = _lib.BArgs()
-    a.precision = _lib.MCL_FP32
-    a.table_steps = (16 * 1024 * 1024 - 256) // 8 + 1
-    assert lib.mcl_b_run_static(C.byref(a), None) == _lib.MCL_ECAPACITY
-    a.precision = _lib.MCL_FP64
-    a.table_steps = (16 * 1024 * 1024 - 256) // 16 + 1
-    assert lib.mcl_b_run_static(C.byref(a), None) == _lib.MCL_ECAPACITY
+    for prec, cap in CAPACITY.items():
+        entry = 16 if prec == _lib.MCL_FP64 else 8
+        assert cap == (16 * 1024 * 1024 - 256) // entry
+        a = _lib.BArgs()
+        a.precision = prec
+        a.table_steps = cap + 1
+        assert lib.mcl_b_run_static(C.byref(a), None) == _lib.MCL_ECAPACITY
+        assert b"static scratch" in lib.mcl_last_error()
+        a.table_steps = cap
+        assert lib.mcl_b_run_static(C.byref(a), None) != _lib.MCL_ECAPACITY
