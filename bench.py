@@ -226,6 +226,7 @@ def main():
     trials = batch.trials
     total_trials = trials * world
     value = total_trials / (ms_max / 1e3)
+    events_per_pass = int(batch.result().lum.sum())
 
     # ---- end to end through the public API (host specs in, host bins out) ----
     e2e = None
@@ -269,6 +270,7 @@ def main():
         "config": {"workload": f"{WORKLOAD}: {a.sets} sets/GPU, ragged 1e3..1e5 traps, "
                                "half TL ramps (0.5-5 K/s to 500 C, dt 0.1 s), half isothermal "
                                "(150-300 C, 1e4 s, dt 1 s)",
+                   "alpha": "rho'^(-1/3) of each set (46..215)", "events_per_pass": events_per_pass,
                    "sets_per_gpu": a.sets, "traps_per_gpu": int(sum(s.n_slots for s in specs)),
                    "trials_per_step_per_gpu": int(trials), "precision": "fp32",
                    "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ,
@@ -280,6 +282,7 @@ def main():
         "gpu_launches_per_step": {"kb_tables": 1, "kb_f32": 1}, "clocks": clk, "roofline": roof,
         "wall_s_timed": t_wall,
     }
+    out["batch_variants"] = variants_bench(a, rank, specs)
     out["dose_fade_irsl"] = sequence_bench(a, rank)
     out["single_set_tl"] = single_set_bench(a, rank, world)
     if not a.no_k:
@@ -298,6 +301,52 @@ def main():
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def variants_bench(a, rank, specs_own):
+    """The headline workload in FP64 (the oracle-parity arithmetic, next to
+    the FP32 headline) and its signal-bearing variant (the same sets with
+    alpha = 5: most TL sets empty by 500 degC) in FP32 and FP64.  Each is the
+    full batch replayed from a captured graph, L2 flushed between passes."""
+    import torch
+    from mcluminescence_gb300 import BernoulliBatch, autotune, schedule
+    sig = schedule.batch_tl_iso(a.sets, seed=a.seed + 7919 * rank, alpha=5.0)
+    for s in sig:
+        s.set_id += rank * a.sets
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, specs in (("own_alpha", specs_own), ("alpha5", sig)):
+        for prec in ("fp32", "fp64"):
+            if name == "own_alpha" and prec == "fp32":
+                continue                      # the headline measurement
+            block, ept, occ = autotune.pick_bernoulli(specs, precision=prec)
+            b = BernoulliBatch(specs, precision=prec, seed=a.seed, block=block, ept=ept,
+                               want_alive=True, occupancy=occ)
+            st = torch.cuda.Stream()
+            b.capture(st)
+            b.replay(st)
+            st.synchronize()
+            reps = 2 if prec == "fp64" else 3
+            ms = []
+            for _ in range(reps):
+                with torch.cuda.stream(st):
+                    flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                b.replay(st)
+                e1.record(st)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            if b.status() != 0:
+                raise RuntimeError(f"kernel status {b.status()}")
+            m = sum(ms) / len(ms)
+            out[f"{name}_{prec}"] = {
+                "alpha": "rho'^(-1/3) of each set" if name == "own_alpha" else 5.0,
+                "precision": prec, "sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": m,
+                "electron_steps_per_s": b.trials / (m / 1e3), "events_per_pass": int(b.result().lum.sum()),
+                "block": block, "ept": ept, "occupancy_build": occ}
+            del b
+    return out
 
 
 def single_set_bench(a, rank, world):

@@ -176,14 +176,18 @@ def single_tl_set(alpha: float = 100.0, n_slots: int = 2000, E: float = 1.45, s:
 
 
 def batch_tl_iso(n_sets: int = 4096, seed: int = 20261203, n_min: int = 1000,
-                 n_max: int = 100000, alpha_from_rho: bool = True) -> List[SetSpec]:
+                 n_max: int = 100000, alpha_from_rho: bool = True,
+                 alpha: Optional[float] = None) -> List[SetSpec]:
     """Batched TL + isothermal workload.
 
     E ~ U[1.2, 1.8] eV, log10 s ~ U[10, 14], rho' log-uniform [1e-7, 1e-5],
     traps per set log-uniform [1e3, 1e5] (ragged); even set ids are TL ramps
     (beta in {0.5, 1, 2, 5} K/s, 0 -> 500 degC, dt = 0.1 s, 1 degC bins), odd
     ids isothermal holds (T ~ U[150, 300] degC, 1e4 s, dt = 1 s, 20 s bins).
-    alpha = rho'^(-1/3).
+    alpha = rho'^(-1/3) (46..215 over the batch: most traps stay filled),
+    10 with ``alpha_from_rho=False``, or the given ``alpha`` for every set
+    (the signal-bearing variant uses 5: most TL sets empty by 500 degC).  The
+    other parameters do not depend on the choice, so the variants share them.
     """
     rng = np.random.default_rng(seed)
     E = rng.uniform(1.2, 1.8, n_sets)
@@ -194,28 +198,33 @@ def batch_tl_iso(n_sets: int = 4096, seed: int = 20261203, n_min: int = 1000,
     T_iso = rng.uniform(150.0, 300.0, n_sets)
     out = []
     for i in range(n_sets):
-        alpha = rho[i] ** (-1.0 / 3.0) if alpha_from_rho else 10.0
+        a_i = alpha if alpha is not None else (rho[i] ** (-1.0 / 3.0) if alpha_from_rho else 10.0)
         if i % 2 == 0:
             seg = tl_ramp(0.0, 500.0, float(betas[i]), 0.1, 1.0)
             kind = "tl"
         else:
             seg = isothermal(float(T_iso[i]), 1e4, 1.0, 20.0)
             kind = "iso"
-        out.append(SetSpec(n_slots=int(n[i]), E=float(E[i]), s=float(s[i]), alpha=float(alpha),
+        out.append(SetSpec(n_slots=int(n[i]), E=float(E[i]), s=float(s[i]), alpha=float(a_i),
                            segments=[seg], set_id=i, kind=kind).finalize())
     return out
 
 
 def batch_dose_fade_irsl(n_sets: int = 2048, seed: int = 20261204, n_min: int = 1000,
                          n_max: int = 100000, fade_steps: int = 200,
-                         s_tun: float = 3e15) -> List[SetSpec]:
+                         s_tun: float = 3e15, alpha: Optional[float] = None) -> List[SetSpec]:
     """Irradiation -> fading -> IRSL sequences (uneven step counts per set).
 
     dose rate ~ U[0.05, 0.2] Gy/s to dose log-uniform [1, 1000] Gy with
     D0 ~ U[100, 500] Gy (fill steps of ~1 s), ground-state tunnelling fading over
     1e5 s in ``fade_steps`` geometric steps, then IR stimulation at 50 degC with
     sigma*Phi log-uniform [1e-3, 1e-1] /s for 1,000 s at dt = 0.1 s.  Traps
-    start empty.  E, s, rho' and alpha as in ``batch_tl_iso``.
+    start empty.  E, s, rho' and alpha as in ``batch_tl_iso``, or the given
+    ``alpha`` for every set.  With alpha = rho'^(-1/3) and s_tun = 3e15 /s
+    the fading empties every trap with alpha r' < ln(3e15 * 1e5) = 48, which
+    includes every trap the stimulation could empty (alpha r' < ln(100)), so
+    the IRSL phase of that workload has no events; a small alpha with a small
+    s_tun (e.g. 5 and 1e-4 /s) gives signal in both phases.
     """
     rng = np.random.default_rng(seed)
     E = rng.uniform(1.2, 1.8, n_sets)
@@ -228,11 +237,11 @@ def batch_dose_fade_irsl(n_sets: int = 2048, seed: int = 20261204, n_min: int = 
     sphi = 10.0 ** rng.uniform(-3.0, -1.0, n_sets)
     out = []
     for i in range(n_sets):
-        alpha = rho[i] ** (-1.0 / 3.0)
+        a_i = alpha if alpha is not None else rho[i] ** (-1.0 / 3.0)
         segs = [irradiate(float(dose[i]), float(rate[i]), float(D0[i]), dt=1.0, T_C=20.0),
                 fade(1e5, fade_steps, s_tun, dt0=1.0, T_C=20.0, steps_per_bin=10),
                 optical(float(sphi[i]), 1000.0, 0.1, T_C=50.0, bin_seconds=1.0)]
         out.append(SetSpec(n_slots=int(n[i]), n_filled=0, E=float(E[i]), s=float(s[i]),
-                           alpha=float(alpha), segments=segs, set_id=i,
+                           alpha=float(a_i), segments=segs, set_id=i,
                            kind="dose_fade_irsl").finalize())
     return out
