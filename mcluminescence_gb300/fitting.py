@@ -14,6 +14,11 @@ candidates of a generation are evaluated together:
                        Monte Carlo noise floor; fits that fail continue with
                        Monte-Carlo-scored DE from the surrogate's population.
 
+Both methods stop each fit on the same criterion: the first Monte Carlo
+evaluation at or below ``accept_factor`` x the fit's noise floor (1.0 by
+default: the expected MSE of the true parameters).  An accepted fit is frozen
+and costs no further Monte Carlo.
+
 The objective is the mean squared difference of area-normalised curves over
 the 200 bins, for the four free parameters (E, log10 s, alpha, log10 rho');
 dose and heating rate are the known experimental conditions.  Targets are
@@ -151,6 +156,11 @@ class DE:
         self.f = self.t.where(better, f_trial, self.f)
 
 
+def _quartiles(r) -> list:
+    r = np.asarray(r, dtype=np.float64)
+    return [float(q) for q in np.quantile(r, [0.25, 0.5, 0.75])] if r.size else []
+
+
 @dataclass
 class FitReport:
     method: str
@@ -164,6 +174,9 @@ class FitReport:
     history: list = field(default_factory=list)
     best_x: object = None         # [F][4] unit-cube parameters of each fit's answer
     reverified_ratio_median: float = float("nan")   # fresh, independent MC of the answers
+    final_ratios: object = None   # [F] MC-verified MSE / floor of each answer
+    reverified_ratios: object = None
+    accept_factor: float = 1.0
 
     @property
     def fits_per_s(self) -> float:
@@ -172,9 +185,13 @@ class FitReport:
     def as_dict(self) -> Dict:
         return {"method": self.method, "seconds": self.seconds, "accepted": self.accepted,
                 "n_fits": self.n_fits, "fits_per_s": self.fits_per_s, "mc_curves": self.mc_curves,
-                "mc_trials": self.mc_trials, "final_mse_over_floor_median": self.final_ratio_median,
+                "mc_trials": self.mc_trials, "accept_factor": self.accept_factor,
+                "final_mse_over_floor_median": self.final_ratio_median,
+                "final_mse_over_floor_quartiles": _quartiles(self.final_ratios if self.final_ratios is not None else []),
                 "accepted_mse_over_floor_median": self.accepted_ratio_median,
-                "reverified_mse_over_floor_median": self.reverified_ratio_median}
+                "reverified_mse_over_floor_median": self.reverified_ratio_median,
+                "reverified_mse_over_floor_quartiles": _quartiles(
+                    self.reverified_ratios if self.reverified_ratios is not None else [])}
 
 
 def _mc_eval(prob: Problem, u, seed: int, id0: int):
@@ -192,29 +209,45 @@ def _steps(full):
     return S.N_BINS * k
 
 
+def _mc_de(prob: Problem, de: DE, thr, max_gens: int, seed: int, id0: int, hist: list, hist_base: int = 0):
+    """Monte-Carlo-scored DE generations until every fit has a member at or
+    below ``thr`` (or ``max_gens``).  A fit that gets there is frozen: its
+    population stops evolving and costs no further Monte Carlo.  ``de.f``
+    must hold the population's Monte Carlo scores.  Returns (curves, trials)."""
+    import torch
+    F, P = de.F, de.P
+    n_curves, n_trials = 0, 0.0
+    done = de.f.min(dim=1).values <= thr
+    for g in range(max_gens):
+        hist.append(hist_base + int(done.sum()))
+        if bool(done.all()):
+            break
+        trial = de.trials()
+        idx = (~done).nonzero().flatten()
+        f_sub, tr = _mc_eval(_subproblem(prob, idx), trial[idx], seed + 17 * (g + 1), id0=id0 + g * F * P)
+        f_trial = torch.full_like(de.f, float("inf"))
+        f_trial[idx] = f_sub
+        n_curves += len(idx) * P
+        n_trials += tr
+        de.select(trial, f_trial)
+        done = done | (de.f.min(dim=1).values <= thr)
+    return n_curves, n_trials
+
+
 def fit_plain_mc(prob: Problem, pop: int = 32, max_gens: int = 60, seed: int = 0,
-                 accept_factor: float = 1.5) -> FitReport:
+                 accept_factor: float = 1.0) -> FitReport:
     import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     F = len(prob.known)
     de = DE(F, pop, FREE, seed)
-    n_curves, n_trials = 0, 0.0
-    de.f, tr = _mc_eval(prob, de.x, seed, id0=1_000_000)
-    n_curves += F * pop
-    n_trials += tr
+    de.f, n_trials = _mc_eval(prob, de.x, seed, id0=1_000_000)
+    n_curves = F * pop
     thr = accept_factor * prob.floor
     hist = []
-    for g in range(max_gens):
-        acc = (de.f.min(dim=1).values <= thr)
-        hist.append(int(acc.sum()))
-        if bool(acc.all()):
-            break
-        trial = de.trials()
-        f_trial, tr = _mc_eval(prob, trial, seed + 17 * (g + 1), id0=2_000_000 + g * F * pop)
-        n_curves += F * pop
-        n_trials += tr
-        de.select(trial, f_trial)
+    c, t = _mc_de(prob, de, thr, max_gens, seed, 2_000_000, hist)
+    n_curves += c
+    n_trials += t
     best = de.f.min(dim=1).values
     best_x = de.x[torch.arange(F, device="cuda"), de.f.argmin(dim=1)]
     acc = best <= thr
@@ -223,7 +256,7 @@ def fit_plain_mc(prob: Problem, pop: int = 32, max_gens: int = 60, seed: int = 0
     ratio = (best / prob.floor).cpu().numpy()
     return FitReport("plain_mc", secs, int(acc.sum()), F, n_curves, n_trials,
                      float(np.median(ratio)), float(np.median(ratio[acc.cpu().numpy()])) if bool(acc.any()) else float("nan"),
-                     hist, best_x)
+                     hist, best_x, final_ratios=ratio, accept_factor=accept_factor)
 
 
 def _surrogate_curves(model, u, known_t):
@@ -266,7 +299,7 @@ def _subproblem(prob: Problem, idx):
 
 def fit_surrogate(prob: Problem, model: "S.SurrogateMLP", pop: int = 32, sur_gens: int = 120,
                   refine_gens: int = 60, verify_top: int = 8, rounds: int = 6, max_mc_gens: int = 60,
-                  seed: int = 0, accept_factor: float = 1.5) -> FitReport:
+                  seed: int = 0, accept_factor: float = 1.0) -> FitReport:
     """Surrogate-proposed, Monte-Carlo-verified fitting.
 
     Round 1: DE on the surrogate for ``sur_gens`` generations, the
@@ -325,17 +358,10 @@ def fit_surrogate(prob: Problem, model: "S.SurrogateMLP", pop: int = 32, sur_gen
         de2.f, tr = _mc_eval(sub, de2.x, seed + 7, id0=8_000_000)
         n_curves += len(open_idx) * pop
         n_trials += tr
-        thr2 = thr[open_idx]
-        for g in range(max_mc_gens):
-            a2 = de2.f.min(dim=1).values <= thr2
-            hist.append(F - len(open_idx) + int(a2.sum()))
-            if bool(a2.all()):
-                break
-            trial = de2.trials()
-            f_trial, tr = _mc_eval(sub, trial, seed + 31 * (g + 1), id0=9_000_000 + g * len(open_idx) * pop)
-            n_curves += len(open_idx) * pop
-            n_trials += tr
-            de2.select(trial, f_trial)
+        c, t = _mc_de(sub, de2, thr[open_idx], max_mc_gens, seed + 14, 9_000_000, hist,
+                      hist_base=F - len(open_idx))
+        n_curves += c
+        n_trials += t
         b2 = de2.f.min(dim=1).values
         x2 = de2.x[torch.arange(len(open_idx), device="cuda"), de2.f.argmin(dim=1)]
         improved = b2 < best[open_idx]
@@ -347,7 +373,7 @@ def fit_surrogate(prob: Problem, model: "S.SurrogateMLP", pop: int = 32, sur_gen
     ratio = (best / prob.floor).cpu().numpy()
     return FitReport("surrogate_mc", secs, int(acc.sum()), F, n_curves, n_trials,
                      float(np.median(ratio)), float(np.median(ratio[acc.cpu().numpy()])) if bool(acc.any()) else float("nan"),
-                     hist, best_x)
+                     hist, best_x, final_ratios=ratio, accept_factor=accept_factor)
 
 
 def reverify(prob: Problem, rep: FitReport, seed: int = 999) -> FitReport:
@@ -355,5 +381,6 @@ def reverify(prob: Problem, rep: FitReport, seed: int = 999) -> FitReport:
     Carlo run (the minimum over a DE population is biased low by the noise of
     the evaluations it was selected on); fills ``reverified_ratio_median``."""
     f, _ = _mc_eval(prob, rep.best_x[:, None, :], seed, id0=90_000_000)
-    rep.reverified_ratio_median = float(np.median((f[:, 0] / prob.floor).cpu().numpy()))
+    rep.reverified_ratios = (f[:, 0] / prob.floor).cpu().numpy()
+    rep.reverified_ratio_median = float(np.median(rep.reverified_ratios))
     return rep

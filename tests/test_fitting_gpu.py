@@ -1,5 +1,6 @@
 """Batched fitting: what the trained surrogate gains over plain Monte Carlo
-fitting at the same Monte-Carlo-verified acceptance criterion."""
+fitting when both stop each fit on the same Monte-Carlo-verified criterion
+(MSE at or below the fit's noise floor, the expected MSE of the truth)."""
 import numpy as np
 import pytest
 
@@ -12,18 +13,24 @@ def test_surrogate_fitting_needs_far_less_monte_carlo():
     m = S.SurrogateMLP(batch=2048, seed=1)
     S.train(m, P, Cn, steps=4000)
     prob = Fm.make_problem(64, seed=22)
-    plain = Fm.fit_plain_mc(prob, pop=32, max_gens=40, seed=3)
-    sur = Fm.fit_surrogate(prob, m, pop=32, seed=3)
+    plain = Fm.fit_plain_mc(prob, pop=32, max_gens=60, seed=3, accept_factor=1.0)
+    sur = Fm.fit_surrogate(prob, m, pop=32, seed=3, accept_factor=1.0)
     Fm.reverify(prob, plain)
     Fm.reverify(prob, sur)
-    # same acceptance criterion (MC-verified MSE within 1.5x the noise floor)
+    # same stopping criterion: every accepted answer's MC-verified MSE <= floor
     assert sur.accepted >= 0.9 * plain.accepted
-    assert sur.accepted >= 0.8 * prob.floor.numel()
+    assert sur.accepted >= 0.9 * prob.floor.numel()
+    acc_s = sur.final_ratios <= 1.0
+    acc_p = plain.final_ratios <= 1.0
+    assert acc_s.sum() == sur.accepted and acc_p.sum() == plain.accepted
     # the surrogate does the search; Monte Carlo only verifies
     assert sur.mc_trials * 3 <= plain.mc_trials, (sur.mc_trials, plain.mc_trials)
-    # the answers hold up under a fresh, independent Monte Carlo run
-    assert sur.reverified_ratio_median < 1.5
-    assert plain.reverified_ratio_median < 1.5
+    # equal quality: under a fresh, independent Monte Carlo run the two
+    # methods' answers score alike (medians within 15 %: with 64 fits the
+    # sampling spread of each median is about 4 %)
+    rs, rp = sur.reverified_ratio_median, plain.reverified_ratio_median
+    assert abs(rs - rp) <= 0.15 * rp, (rs, rp)
+    assert rs < 1.5 and rp < 1.5
 
 
 def test_plain_fit_recovers_hidden_parameters_on_easy_targets():
