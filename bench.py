@@ -436,11 +436,13 @@ def kinetics_k_bench(a, rank, world):
     from mcluminescence_gb300.config import default_config, initialize_runs
     cfg = default_config()
     np.random.seed(a.seed)
-    K.simulate(cfg)                               # warm-up (module load)
+    # CSV side effect off: the reference times recorded with the fixtures
+    # exclude it too (its stand-in pandas wrote nothing there)
+    K.simulate(cfg, write_csv=False)              # warm-up (module load)
     torch.cuda.synchronize()
     np.random.seed(a.seed)
     t0 = time.perf_counter()
-    (x_ax, lum, ratio, configs), res = K.simulate(cfg, return_result=True)
+    (x_ax, lum, ratio, configs), res = K.simulate(cfg, return_result=True, write_csv=False)
     torch.cuda.synchronize()
     compat_s = time.perf_counter() - t0
     runs = initialize_runs(cfg)
@@ -471,11 +473,11 @@ def kinetics_k_bench(a, rank, world):
         gcfg = json.loads(bytes(gold[f"{case}/cfg"]).decode())
         seed = int(gold[f"{case}/seed"])
         np.random.seed(seed)
-        K.simulate(gcfg)
+        K.simulate(gcfg, write_csv=False)
         torch.cuda.synchronize()
         np.random.seed(seed)
         t0 = time.perf_counter()
-        g_x, g_lum, g_ratio, _ = K.simulate(gcfg)
+        g_x, g_lum, g_ratio, _ = K.simulate(gcfg, write_csv=False)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         ref_s = float(gold[f"{case}/wall_s"])
@@ -503,8 +505,8 @@ def fitting_bench(a, rank):
     """Surrogate training on device-generated Monte Carlo curves (1M curves,
     6 -> 256x4 -> 200 GELU MLP, batch 4096, Adam), then 1,024 simultaneous fits
     of Poisson-noised Monte Carlo targets: surrogate-proposed / MC-verified
-    versus plain-MC differential evolution at the same acceptance criterion
-    (MC-verified MSE <= 1.5 x the noise floor)."""
+    versus plain-MC differential evolution, both stopping each fit at the same
+    criterion (MC-verified MSE <= 1.0 x the noise floor)."""
     import numpy as np
     import torch
     from mcluminescence_gb300 import fitting as Fm, surrogate as S
@@ -524,10 +526,12 @@ def fitting_bench(a, rank):
     warm = Fm.make_problem(8, seed=a.seed + 6)            # load every kernel before timing
     Fm.fit_surrogate(warm, m, seed=0, rounds=1, sur_gens=2, max_mc_gens=1)
     Fm.fit_plain_mc(warm, max_gens=1, seed=0)
-    sur = Fm.reverify(prob, Fm.fit_surrogate(prob, m, seed=1))
+    sur = Fm.reverify(prob, Fm.fit_surrogate(prob, m, seed=1, accept_factor=1.0))
     sub = Fm._subproblem(prob, torch.arange(min(a.plain_fits, a.fits), device="cuda"))
-    plain = Fm.reverify(sub, Fm.fit_plain_mc(sub, pop=32, max_gens=60, seed=1))
+    plain = Fm.reverify(sub, Fm.fit_plain_mc(sub, pop=32, max_gens=60, seed=1, accept_factor=1.0))
     train_s = t2 - t0
+    # the same fits answered by the surrogate path, for a like-for-like median
+    sur_sub_rev = float(np.median(sur.reverified_ratios[:sub.floor.numel()]))
     return {
         "surrogate": {"train_curves": len(P), "datagen_s": t1 - t0, "train_steps": 8000,
                       "train_s": t2 - t1, "loss_history": hist,
@@ -536,8 +540,13 @@ def fitting_bench(a, rank):
         "fits_per_s_ratio": sur.fits_per_s / plain.fits_per_s if plain.fits_per_s else None,
         "mc_trials_per_fit_ratio": (plain.mc_trials / plain.n_fits) / (sur.mc_trials / sur.n_fits),
         "surrogate_fits_per_s_incl_training": sur.accepted / (sur.seconds + train_s),
-        "acceptance": "MC-verified MSE of area-normalised curves <= 1.5 x noise floor "
-                      "(Poisson at ~1e4 peak counts + 20,000-trap Monte Carlo)",
+        "reverified_median_rel_diff": (sur.reverified_ratio_median - plain.reverified_ratio_median)
+        / plain.reverified_ratio_median,
+        "surrogate_reverified_median_on_plain_fits": sur_sub_rev,
+        "acceptance": "both methods stop each fit at its first Monte Carlo evaluation with MSE of "
+                      "area-normalised curves <= 1.0 x its noise floor (the expected MSE of the true "
+                      "parameters: Poisson at ~1e4 peak counts + 20,000-trap Monte Carlo); "
+                      "'reverified' scores each answer again with a fresh, independent Monte Carlo run",
     }
 
 

@@ -289,6 +289,35 @@ int mcl_k_run(const mcl_k_args* args, void* stream);
 int64_t mcl_k_region_bytes(int32_t e_cap, int32_t h_cap, int32_t arrays_in_smem);
 int32_t mcl_k_arrays_fit_smem(int32_t e_cap_max, int32_t h_cap_max);
 
+/* ---- step-level operations of the event-driven loop ------------------------ */
+/* For callers that drive the loop one step at a time through the reference's
+ * TLTrapSim / Box surface (src/class/simulate.py:51-92); mcl_k_run keeps the
+ * whole loop on the device and is the throughput path.  Coordinates are
+ * device arrays [n][3] (FP64, row-major).
+ * mcl_k_box_nearest replaces Box._rebuild / the incremental searches of
+ * Box.add_electron and Box.remove_pair (src/class/engine.py:113-119, 147-152,
+ * 170-175): for each electron index in rows[0..n_rows) (all n_e electrons
+ * when rows is NULL and n_rows == n_e), the minimum over the n_h holes of
+ * sqrt((dx*dx + dy*dy) + dz*dz), dx = e.x - h.x (numpy's np.linalg.norm
+ * association, no contraction) into min_d[row] and its first argmin into
+ * nearest[row]; a NaN distance counts as the minimum, as in numpy; row
+ * indices outside [0, n_e) are skipped.  n_h == 0
+ * with n_rows > 0 returns MCL_ENOHOLE (numpy raises ValueError there). */
+int mcl_k_box_nearest(const double* electrons, int32_t n_e, const double* holes, int32_t n_h,
+                      const int32_t* rows, int32_t n_rows, double* min_d, int64_t* nearest, void* stream);
+/* TLTrapSim._update_lifetimes (src/class/tl_trap_lab.py:48-51 over
+ * src/class/engine.py:65-77) given its uniforms: E_loc = E_loc_2 if
+ * u_retrap[i] < Retrap else E_loc_1; lifetime[i] = 1 / (s exp(-E_cb/(k_b T))
+ * + b exp(-E_loc/(k_b T) - alpha min_d[i])); wait[i] = lifetime[i] *
+ * (-log(1 - u_wait[i])) (numpy's legacy exponential).  The physics fields of
+ * *phys (a host struct) are read; the rest of it is ignored. */
+int mcl_k_box_waits(const mcl_k_sim* phys, double T, const double* min_d, const double* u_retrap,
+                    const double* u_wait, int32_t n, double* lifetime, double* wait, void* stream);
+/* Box.distances (src/class/engine.py:180-183): out[i*n_h + j] = the distance
+ * of electron i to hole j, as mcl_k_box_nearest evaluates it. */
+int mcl_k_box_distances(const double* electrons, int32_t n_e, const double* holes, int32_t n_h, double* out,
+                        void* stream);
+
 /* ---- surrogate network (no counterpart in the reference) ------------------ */
 /* The reference fits parameters by running the Monte Carlo for every
  * candidate (src/class/optimizer.py:93-111); these kernels train and run a

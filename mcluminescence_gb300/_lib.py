@@ -142,6 +142,9 @@ def _declare(lib):
         "mcl_f32_to_bf16": (C.c_int, [i64, vp, vp, vp]),
         "mcl_adam_multi": (C.c_int, [vp, i32, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]),
         "mcl_adam_multi_dev": (C.c_int, [vp, i32, vp, vp, i32, C.c_float, C.c_float, C.c_float, vp]),
+        "mcl_k_box_nearest": (C.c_int, [vp, i32, vp, i32, vp, i32, vp, vp, vp]),
+        "mcl_k_box_waits": (C.c_int, [vp, C.c_double, vp, vp, vp, i32, vp, vp, vp]),
+        "mcl_k_box_distances": (C.c_int, [vp, i32, vp, i32, vp, vp]),
         "mcl_k_region_bytes": (i64, [i32, i32, i32]),
         "mcl_k_arrays_fit_smem": (i32, [i32, i32]),
         "mcl_glow_extent": (C.c_int, [vp, i32, i32, i32, vp, vp, C.c_double, vp, vp]),
@@ -164,7 +167,8 @@ EXPORTS = (
     "mcl_graph_destroy", "mcl_bench_philox", "mcl_b_run_static", "mcl_k_validate", "mcl_k_run",
     "mcl_gemm_nt", "mcl_gemm_nt_tc", "mcl_act_backward", "mcl_mse_loss", "mcl_adam", "mcl_f32_to_bf16",
     "mcl_glow_extent", "mcl_glow_hist", "mcl_running_mean", "mcl_adam_multi", "mcl_adam_multi_dev",
-    "mcl_k_region_bytes", "mcl_k_arrays_fit_smem",
+    "mcl_k_region_bytes", "mcl_k_arrays_fit_smem", "mcl_k_box_nearest", "mcl_k_box_waits",
+    "mcl_k_box_distances",
 )
 
 

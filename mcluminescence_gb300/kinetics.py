@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import csv
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import Any, Dict, List, Optional, Sequence
 
@@ -277,8 +278,15 @@ def _raise_for(status: np.ndarray, steps: int):
             raise _lib.MclError(code, "event-driven kinetics kernel", detail=False)
 
 
+def results_dir() -> str:
+    """Where ``simulate`` writes its table: ``MCL_RESULTS_DIR`` if set, else
+    ``results/simulations`` under the current directory (the reference
+    writes under its project root, src/class/simulate.py:110)."""
+    return os.environ.get("MCL_RESULTS_DIR") or os.path.join(os.getcwd(), "results", "simulations")
+
+
 def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,
-             dose_rate: Optional[float] = None, csv_path: Optional[str] = None,
+             dose_rate: Optional[float] = None, write_csv: bool = True, csv_path: Optional[str] = None,
              block: Optional[int] = None, return_result: bool = False):
     """GPU replacement of src/class/simulate.py:simulate.
 
@@ -286,7 +294,10 @@ def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,
     ``seed`` first when given); ``rng="philox"`` uses independent Philox
     streams keyed by ``seed``.  ``dose_rate`` switches trap filling on (the
     reference reads it from ``physics_fp.dose_rate``, a key its Physics class
-    rejects).  ``csv_path`` writes the long table of simulate.py:95-110.
+    rejects).  Like the reference, the call writes the long table of
+    simulate.py:95-110 to ``exp_{tag}.csv`` (``tag`` = ``cfg.tag``, default
+    "") in ``results_dir()``, creating the directory; ``csv_path`` gives
+    another file, ``write_csv=False`` turns the side effect off.
     """
     configs = initialize_runs(cfg)
     n_runs = len(configs)
@@ -318,32 +329,61 @@ def simulate(cfg: Any, *, rng: str = "numpy", seed: Optional[int] = None,
     x_ax = res.x_ax.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
     lum = res.lum.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
     ratio = res.electron_ratio.reshape(steps, n_runs, sims).transpose(0, 2, 1).copy()
-    if csv_path:
+    if write_csv or csv_path:
+        if not csv_path:
+            os.makedirs(results_dir(), exist_ok=True)
+            csv_path = os.path.join(results_dir(), f"exp_{_get(cfg, 'tag', '')}.csv")
         write_table(csv_path, lum, ratio)
     out = (x_ax, lum, ratio, configs)
     return (out, res) if return_result else out
 
 
 def write_table(path: str, lum: np.ndarray, ratio: np.ndarray) -> None:
-    """Long table run,sim,step,lum,electron_ratio (src/class/simulate.py:95-110)."""
+    """The long table of src/class/simulate.py:95-110, byte for byte: columns
+    run,sim,step,lum,electron_ratio, rows ordered run, then sim, then step
+    (the tables transposed to (runs, sims, steps) and flattened), written the
+    way the reference's ``DataFrame.to_csv(path, index=False)`` writes them
+    (pandas 2.2.3, requirements.txt:14): integers as ``str``, float64 values
+    as numpy's shortest round-trip repr (``astype(str)``), commas, and
+    ``os.linesep`` after every line including the header."""
     steps, sims, runs = lum.shape
+    cols = (np.repeat(np.arange(runs), sims * steps).astype(str),
+            np.tile(np.repeat(np.arange(sims), steps), runs).astype(str),
+            np.tile(np.arange(steps), runs * sims).astype(str),
+            np.ascontiguousarray(lum.transpose(2, 1, 0)).ravel().astype(str),
+            np.ascontiguousarray(ratio.transpose(2, 1, 0)).ravel().astype(str))
+    comma = np.array(",")
+    rows = cols[0]
+    for c in cols[1:]:
+        rows = np.char.add(np.char.add(rows, comma), c)
+    nl = os.linesep
     with open(path, "w", newline="") as f:
-        w = csv.writer(f)
-        w.writerow(["run", "sim", "step", "lum", "electron_ratio"])
-        for r in range(runs):
-            for s in range(sims):
-                for k in range(steps):
-                    w.writerow([r, s, k, repr(float(lum[k, s, r])), repr(float(ratio[k, s, r]))])
+        f.write("run,sim,step,lum,electron_ratio" + nl)
+        if rows.size:
+            f.write(nl.join(rows.tolist()) + nl)
 
 
 # ---------------------------------------------------------------------------
 # lab-data objectives: the TLTrapSim drop-in (tl_trap_lab.py:24-179)
 # ---------------------------------------------------------------------------
+def data_dir() -> str:
+    """Where lab tables named without a path are found: ``MCL_DATA_DIR`` if
+    set, else ``data/processed`` under the project root (``MCL_PROJECT_ROOT``
+    or the current directory), as the reference reads
+    ``PROJECT_ROOT/data/processed/<name>.csv`` (tl_trap_lab.py:67, 127)."""
+    root = os.environ.get("MCL_PROJECT_ROOT") or os.getcwd()
+    return os.environ.get("MCL_DATA_DIR") or os.path.join(root, "data", "processed")
+
+
 def read_table(src) -> Dict[str, np.ndarray]:
-    """A lab table as columns: a dict of columns, or a CSV path (the reference
-    reads data/processed/<name>.csv with pandas)."""
+    """A lab table as columns: a dict of columns, a CSV path, or a table
+    name (no directory, no extension) looked up in ``data_dir()`` like the
+    reference's ``TL_lab(csv_name)``."""
     if isinstance(src, dict):
         return {k: np.asarray(v) for k, v in src.items()}
+    src = str(src)
+    if os.sep not in src and not src.endswith(".csv"):
+        src = os.path.join(data_dir(), src + ".csv")
     with open(src, newline="") as f:
         rows = list(csv.DictReader(f))
     out = {}
@@ -356,31 +396,228 @@ def read_table(src) -> Dict[str, np.ndarray]:
     return out
 
 
-class TLTrapSim:
-    """GPU drop-in of src/class/tl_trap_lab.py:TLTrapSim for its lab objectives.
+class _Attr(dict):
+    """A config group or the physics constants with attribute access
+    (``sim.mc.N_e``, ``sim.phys.D0``), as the reference's DictConfig and
+    Physics objects give it."""
 
-    The constructor performs the reference's checks (``Physics(**physics_fp)``)
-    and, with ``rng="numpy"``, consumes the uniforms the reference's
-    constructor draws to seed its box (engine.py:124-129), so
-    ``np.random.seed(k); TLTrapSim(run).TL_lab(table)`` matches the reference.
-    ``TL_lab`` and ``ISO_lab`` take a lab table (dict of columns or a CSV path
-    with the reference's columns) and return the MSE like the reference.
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+
+def _empty_min():
+    return ValueError("zero-size array to reduction operation minimum which has no identity")
+
+
+class Box:
+    """GPU-backed drop-in of src/class/engine.py:Box (electrons, recombination
+    centres and the nearest-centre bookkeeping), for callers that step the
+    simulation themselves.
+
+    Coordinates are drawn from ``rng`` (numpy's global legacy stream unless
+    another ``RandomState`` is given) in the reference's order and kept as
+    host arrays ``electrons`` / ``holes`` like the reference's.  Every
+    distance is evaluated on the GPU (``mcl_k_box_nearest``,
+    ``mcl_k_box_distances``) exactly as np.linalg.norm evaluates it, and the
+    bookkeeping follows engine.py:113-188 step for step, quirks included:
+    ``seed`` invalidates the distance cache but not the nearest arrays; a new
+    electron's nearest centre is searched over the centres that existed
+    before its own (engine.py:147,151-152) and existing electrons ignore the
+    new centre; ``remove_pair`` shifts the nearest indices above the removed
+    centre before it masks the owners of that index, so the former owners of
+    the next centre are searched again too (engine.py:167-175); without a
+    cache ``remove_pair`` only deletes coordinates.  The full distance
+    matrix is not kept: every search recomputes the distances it needs,
+    which gives the values the reference caches.
+    """
+
+    def __init__(self, L: float, W: float, H: float, boundary_factor: float, rng=None):
+        self.L, self.W, self.H, self.boundary_factor = L, W, H, boundary_factor
+        self._rs = rng if rng is not None else np.random
+        self.electrons = np.zeros((0, 3))
+        self.holes = np.zeros((0, 3))
+        self._cached = False      # the reference's `_d is not None`
+        self._min_d = None
+        self._nearest = None
+
+    @property
+    def core_shape(self):
+        return self.L, self.W, self.H
+
+    @property
+    def boundary_shape(self):
+        bf = self.boundary_factor
+        return self.L * bf, self.W * bf, self.H * bf
+
+    @staticmethod
+    def _dev(a):
+        import torch
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+    def _search(self, electrons, holes, rows=None):
+        """(min distance, first argmin) over ``holes`` of the listed rows of
+        ``electrons`` (all rows if None), on the GPU."""
+        import torch
+        lib = _lib.load()
+        n_e, n_h = int(electrons.shape[0]), int(holes.shape[0])
+        rows = np.arange(n_e) if rows is None else np.asarray(rows)
+        if rows.size == 0:
+            return np.zeros(0), np.zeros(0, dtype=np.int64)
+        if n_h == 0:
+            raise _empty_min()
+        d_e, d_h = self._dev(electrons), self._dev(holes)
+        d_rows = torch.from_numpy(rows.astype(np.int32)).cuda()
+        md = torch.empty(n_e, dtype=torch.float64, device="cuda")
+        nn = torch.empty(n_e, dtype=torch.int64, device="cuda")
+        st = torch.cuda.current_stream()
+        _lib.check(lib.mcl_k_box_nearest(_lib.ptr(d_e), n_e, _lib.ptr(d_h), n_h, _lib.ptr(d_rows), int(rows.size),
+                                         _lib.ptr(md), _lib.ptr(nn), C.c_void_p(st.cuda_stream)),
+                   "mcl_k_box_nearest")
+        return md.cpu().numpy()[rows], nn.cpu().numpy()[rows]
+
+    def _rebuild(self) -> None:
+        self._min_d, self._nearest = self._search(self.electrons, self.holes)
+        self._cached = True
+
+    def seed(self, n_e: int, n_h: int) -> None:
+        self.electrons = self._rs.rand(n_e, 3) * self.core_shape
+        total_h = int(n_h * self.boundary_factor ** 3)
+        self.holes = self._rs.rand(total_h, 3) * self.boundary_shape
+        self._cached = False
+
+    def add_electron(self) -> None:
+        new_e = self._rs.rand(1, 3) * self.core_shape
+        new_h = self._rs.rand(1, 3) * self.boundary_shape
+        old_holes = self.holes
+        self.electrons = np.vstack([self.electrons, new_e])
+        self.holes = np.vstack([self.holes, new_h])
+        if not self._cached:
+            self._rebuild()
+            return
+        md, nn = self._search(new_e, old_holes)
+        self._min_d = np.append(self._min_d, md)
+        self._nearest = np.append(self._nearest, nn)
+
+    def remove_pair(self, e_idx: int, h_idx: int) -> None:
+        self.electrons = np.delete(self.electrons, e_idx, axis=0)
+        self.holes = np.delete(self.holes, h_idx, axis=0)
+        if not self._cached:
+            return
+        self._min_d = np.delete(self._min_d, e_idx)
+        self._nearest = np.delete(self._nearest, e_idx)
+        self._nearest[self._nearest > h_idx] -= 1
+        mask = self._nearest == h_idx
+        if mask.any():
+            md, nn = self._search(self.electrons, self.holes, np.nonzero(mask)[0])
+            self._min_d[mask] = md
+            self._nearest[mask] = nn
+
+    def distances(self) -> np.ndarray:
+        """The electron x centre distance matrix (computed on the GPU)."""
+        import torch
+        if not self._cached:
+            self._rebuild()
+        n_e, n_h = self.electrons.shape[0], self.holes.shape[0]
+        out = torch.empty(n_e * n_h, dtype=torch.float64, device="cuda")
+        if n_e * n_h:
+            # the device copies stay referenced until the result is read back
+            d_e, d_h = self._dev(self.electrons), self._dev(self.holes)
+            _lib.check(_lib.load().mcl_k_box_distances(
+                _lib.ptr(d_e), n_e, _lib.ptr(d_h), n_h, _lib.ptr(out),
+                C.c_void_p(torch.cuda.current_stream().cuda_stream)), "mcl_k_box_distances")
+        return out.cpu().numpy().reshape(n_e, n_h)
+
+    def nearest(self):
+        if self._min_d is None:
+            self._rebuild()
+        return self._min_d, self._nearest
+
+
+class TLTrapSim:
+    """GPU drop-in of src/class/tl_trap_lab.py:TLTrapSim.
+
+    The constructor performs the reference's checks (``Physics(**physics_fp)``),
+    sizes the box as tl_trap_lab.py:33-35 does and seeds it (engine.py:124-129)
+    from numpy's global stream (``rng="numpy"``), so ``np.random.seed(k);
+    TLTrapSim(run).TL_lab(table)`` matches the reference.  ``TL_lab`` and
+    ``ISO_lab`` take a lab table (dict of columns or a CSV path with the
+    reference's columns) and return the MSE like the reference; they run the
+    whole loop in one launch.
+
+    The step-level surface that the reference's ``simulate()`` loop drives
+    (simulate.py:51-92) is here too: ``box`` (a GPU-backed ``Box``),
+    ``_update_lifetimes(T)`` (lifetimes and waits on the GPU from the
+    reference's draws), ``_filling_time(D)``, ``_lifetime``,
+    ``_recomb_wait``, ``mc`` and ``phys`` with attribute access.  It takes
+    one GPU round trip per call; ``simulate(cfg)`` runs the same loop in one
+    launch and is the throughput path.  With ``rng="philox"`` the box and the
+    step-level draws use a private numpy generator seeded with ``seed``.
     """
 
     def __init__(self, cfg: Any, *, e_ratio_start: Optional[float] = None, rng: str = "numpy",
                  seed: Optional[int] = None, block: Optional[int] = None):
         self.cfg = cfg
-        self.mc = cfg["exp_type_fp"]
-        self.phys = physics(cfg["physics_fp"])
+        mc = cfg["exp_type_fp"]
+        self.mc = _Attr(mc) if isinstance(mc, dict) else mc
+        self.phys = _Attr(physics(cfg["physics_fp"]))
         self.D = _get(cfg["physics_fp"], "D", None)
         self.rng, self.seed, self.block = rng, seed, block
         self.last = None
-        e0 = int(self.mc["N_e"] * (e_ratio_start if e_ratio_start is not None else 0))
-        total_h = int(self.mc["holes"] * self.mc["boundary_factor"] ** 3)
         if rng == "numpy":
             if seed is not None:
                 np.random.seed(seed)
-            np.random.random_sample(3 * e0 + 3 * total_h)
+            self._rs = np.random
+        else:
+            self._rs = np.random.RandomState(seed or 0)
+        rho = self.mc["rho_prime"] * (3 / (4 * np.pi) * self.phys["alpha"] ** 3)
+        d = (self.mc["holes"] / rho) ** (1 / 3)
+        self.box = Box(d, d, d, self.mc["boundary_factor"], rng=self._rs)
+        e0 = int(self.mc["N_e"] * (e_ratio_start if e_ratio_start is not None else 0))
+        self.box.seed(e0, self.mc["holes"])
+        self._lifetime = None
+        self._recomb_wait = None
+        self._k_phys = None
+
+    def _update_lifetimes(self, T: float) -> None:
+        """tl_trap_lab.py:48-51: fresh lifetimes at temperature T (K) and an
+        exponential wait per electron.  The uniforms come from the stream in
+        the reference's order -- the Retrap choices (engine.py:72), then the
+        waits' -- and the arithmetic runs on the GPU (mcl_k_box_waits)."""
+        import torch
+        d_min, _ = self.box.nearest()
+        n = int(d_min.shape[0])
+        u_r = self._rs.random_sample(n)
+        u_w = self._rs.random_sample(n)
+        if self._k_phys is None:
+            self._k_phys = np.zeros(1, dtype=K_SIM_DTYPE)
+            for k, v in self.phys.items():
+                self._k_phys[0][k] = v
+        if n == 0:
+            self._lifetime, self._recomb_wait = np.zeros(0), np.zeros(0)
+            return
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+        d_d, d_r, d_w = dev(d_min), dev(u_r), dev(u_w)
+        lt = torch.empty(n, dtype=torch.float64, device="cuda")
+        wt = torch.empty(n, dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().mcl_k_box_waits(
+            _lib.ptr(self._k_phys), float(T), _lib.ptr(d_d), _lib.ptr(d_r), _lib.ptr(d_w), n, _lib.ptr(lt),
+            _lib.ptr(wt), C.c_void_p(torch.cuda.current_stream().cuda_stream)), "mcl_k_box_waits")
+        self._lifetime = lt.cpu().numpy()
+        self._recomb_wait = wt.cpu().numpy()
+
+    def _filling_time(self, D: float) -> float:
+        """tl_trap_lab.py:53-60: the wait for the next filling event (one
+        draw from the stream on every call)."""
+        e = self.box.electrons.shape[0]
+        N = int(self.mc["N_e"])
+        if e == N or D == 0:
+            lam = 1e-20
+        else:
+            lam = (D / self.phys["D0"]) * (N - e)
+        return self._rs.exponential(1 / lam) if lam > 0 else 1e20
 
     def _params(self, e_ratio, T_start_C, T_rate, duration, D, loop, obs=None) -> RunParams:
         run = {"exp_type_fp": dict(self.mc), "physics_fp": dict(self.cfg["physics_fp"])}

@@ -10,6 +10,10 @@ if REPO not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built library")
+    # simulate() writes its long table like the reference does; keep the
+    # tests' tables out of the working tree
+    import tempfile
+    os.environ.setdefault("MCL_RESULTS_DIR", tempfile.mkdtemp(prefix="mcl_results_"))
 
 
 def pytest_collection_modifyitems(config, items):

@@ -1,7 +1,14 @@
 """Stand-in for the parts of pandas the reference's src/class touches.
 
-``DataFrame.to_csv`` is a no-op (the reference writes into its own read-only
-tree).  ``read_csv`` serves tables registered with ``register_table`` by the
+``DataFrame.to_csv`` writes nothing unless ``MCL_REFSHIM_CSV_DIR`` names a
+directory: the reference writes into its own tree, which may be read-only,
+so the file goes to that directory under the same base name.  The text
+follows pandas 2.2.3 (the reference's pin, requirements.txt:14) for what the
+reference writes (``to_csv(path, index=False)`` of integer and float64
+columns): the column names joined by commas, then one line per row with
+each integer column as ``str(int)`` and each float64 column as numpy's
+``astype(str)`` (the shortest repr that round-trips), joined by commas,
+every line ended by ``os.linesep``.  ``read_csv`` serves tables registered with ``register_table`` by the
 fixture generator (synthetic lab tables), so the reference's TL_lab / ISO_lab
 run unmodified on them.  The DataFrame supports what those methods use:
 ``iterrows`` with attribute access, column attributes with ``mean``,
@@ -77,7 +84,17 @@ class DataFrame(dict):
         for i in range(n):
             yield i, _Row({k: np.asarray(v)[i].item() for k, v in self.items()})
 
-    def to_csv(self, *a, **k):
+    def to_csv(self, path=None, *a, index=True, **k):
+        out_dir = os.environ.get("MCL_REFSHIM_CSV_DIR")
+        if not out_dir or path is None:
+            return None
+        if index:
+            raise NotImplementedError("the stand-in writes index=False tables only")
+        cols = list(self.keys())
+        text = [np.asarray(self[c]).astype(str) for c in cols]
+        lines = [",".join(cols)] + [",".join(t[i] for t in text) for i in range(len(text[0]) if text else 0)]
+        with open(os.path.join(out_dir, os.path.basename(str(path))), "w", newline="") as f:
+            f.write(os.linesep.join(lines) + os.linesep)
         return None
 
 
