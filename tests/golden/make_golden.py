@@ -286,8 +286,63 @@ def run_lab(kind, seed):
     return out
 
 
+def _read_columns(path):
+    """A CSV of numbers as {column: float array}, empty cells as NaN (what
+    pandas' read_csv gives for these files)."""
+    import csv
+    with open(path, newline="") as f:
+        rows = list(csv.DictReader(f))
+    return {k: np.array([float(r[k]) if r[k] not in ("", None) else np.nan for r in rows])
+            for k in rows[0] if k}
+
+
+# The reference's optimiser in replay mode on its own lab data: the
+# min-MSE row of results/lab_sims/result_tl_clbr.csv (optimizer.py:124-132)
+# scored by the reference's objective (optimizer.py:82-84 -> run_one_sim ->
+# TLTrapSim.TL_lab) against data/processed/CLBR_IRSL50_0.25KperGy.csv, with
+# the lab configuration groups.
+REAL_LAB = {"replay_tl_clbr": ("tl_clbr", "CLBR_IRSL50_0.25KperGy", "result_tl_clbr.csv", 41)}
+
+
+def run_lab_real(name):
+    import pandas as stub_pd
+    import optimizer as ref_opt
+    exp, table_name, result_name, seed = REAL_LAB[name]
+    table = _read_columns(os.path.join(REF, "data", "processed", table_name + ".csv"))
+    stub_pd.register_table(table_name, table)
+    res_cols = _read_columns(os.path.join(REF, "results", "lab_sims", result_name))
+    mse_col = res_cols["mse"]
+    best = int(np.nanargmin(mse_col))   # pandas idxmin: the first minimum, NaN skipped
+    best_p = np.array([res_cols[f"param_{i}"][best] for i in range(10)], dtype=np.float64)
+    cfg_plain = compose(CONF, ["physics_fp=lab_TL", "exp_type_fp=TLlab"])
+    cfg = OmegaConf.create(cfg_plain)
+    LOG["sims"] = []
+    _draws[0] = 0
+    np.random.seed(seed)
+    t0 = time.time()
+    mse = ref_opt.objective(best_p, cfg, exp)
+    wall = time.time() - t0
+    sims = LOG["sims"]          # the first is the objective's TLTrapSim constructor
+    draws = []
+    for i, s in enumerate(sims):
+        end = sims[i + 1]["draw0"] if i + 1 < len(sims) else _draws[0]
+        draws.append(end - s["draw0"])
+    out = {f"{name}/cfg": np.frombuffer(json.dumps(cfg_plain).encode(), dtype=np.uint8),
+           f"{name}/table": np.frombuffer(json.dumps({k: v.tolist() for k, v in table.items()}).encode(),
+                                          dtype=np.uint8),
+           f"{name}/results_mse": mse_col.astype(np.float64), f"{name}/best_params": best_p,
+           f"{name}/exp": np.array(exp), f"{name}/seed": np.array(seed), f"{name}/mse": np.array(mse),
+           f"{name}/n_sims": np.array(len(sims)), f"{name}/draws": np.array(draws, dtype=np.int64),
+           f"{name}/wall_s": np.array(wall)}
+    for i, s in enumerate(sims):
+        out[f"{name}/events{i}"] = np.array(s["events"], dtype=np.int64).reshape(-1, 4)
+    print(f"{name}: mse {mse:.6g}, {len(sims)} sims, events {[len(s['events']) for s in sims]}, "
+          f"draws {draws}, {wall:.1f}s", flush=True)
+    return out
+
+
 def main(argv):
-    names = argv[1:] or list(CASES) + ["box_ops", "lab_tl", "lab_iso"]
+    names = argv[1:] or list(CASES) + ["box_ops", "lab_tl", "lab_iso"] + list(REAL_LAB)
     path = os.path.join(HERE, "kinetics_k.npz")
     data = dict(np.load(path)) if os.path.exists(path) else {}
     for n in names:
@@ -296,6 +351,8 @@ def main(argv):
             data.update(run_box_ops())
         elif n in ("lab_tl", "lab_iso"):
             data.update(run_lab(n[4:], seed=31 if n == "lab_tl" else 32))
+        elif n in REAL_LAB:
+            data.update(run_lab_real(n))
         else:
             data.update(run_case(n, CASES[n]))
     np.savez_compressed(path, **data)

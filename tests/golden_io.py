@@ -12,7 +12,10 @@ def load_k():
 
 
 def k_case_names(data):
-    return sorted({k.split("/")[0] for k in data.files if k.endswith("/cfg")})
+    """The simulate() cases: those that stored the reference's output tables
+    (the lab-objective and replay cases store an MSE instead)."""
+    return sorted({k.split("/")[0] for k in data.files if k.endswith("/cfg")
+                   and f"{k.split('/')[0]}/x_ax" in data.files})
 
 
 def k_case(data, name):
