@@ -339,6 +339,57 @@ int mcl_gemm_nt(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A
 int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                    const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
                    int32_t ldy, void* Yt, int32_t ldyt, int32_t* err, void* stream);
+/* The whole network in one persistent launch: one CTA per 128-row tile of
+ * the batch keeps the tile's activations in shared memory and its
+ * accumulator in tensor memory from layer to layer (tcgen05 MMAs with
+ * M 128, N 256, K 16), copying each layer's weights from L2 while the
+ * previous layer's epilogue runs.  Forward: bias + GELU epilogues, the last
+ * layer's outputs to `out`.  Training adds, in the same launch and per
+ * tile, the loss and its gradient (mcl_mse_loss's), then the input-gradient
+ * chain dY_{l-1} = dZ_l W_l with dZ = dY * GELU'(pre-activation) fused into
+ * the epilogues (mcl_act_backward's), writing what the weight gradients
+ * need (the transposed activations and dZ) and adding the bias gradients.
+ * The weight gradients then take one mcl_gemm_nt_tc_grouped launch.  The
+ * network shape is fixed: 6 inputs (padded to 64), four hidden layers of
+ * 256, 200 outputs (padded to 256). */
+typedef struct mcl_mlp_layer {
+  const void* W;        /* bf16 [256][k] (k = 64 for layer 0, else 256)        */
+  const void* Wt;       /* bf16 [k][256] (training, layers 1..4)               */
+  const float* bias;    /* [256]                                               */
+  float* grad_b;        /* [256] += bias gradient (training; caller clears)    */
+  void* dZt;            /* bf16 [256][batch] d loss / d pre-activation, transposed (training) */
+  float* gelu_grad;     /* [batch][256] GELU' of the pre-activation (training, layers 0..3) */
+  void* Yt;             /* bf16 [256][batch] activation, transposed (training, layers 0..3) */
+} mcl_mlp_layer;
+
+typedef struct mcl_mlp_args {
+  mcl_mlp_layer layer[5];
+  const float* x;       /* [*][6] standardized inputs                           */
+  const int64_t* idx;   /* [batch] rows of x and target to use, or NULL (rows 0..batch-1) */
+  const float* target;  /* [*][target_ld], 200 used per row (training)          */
+  float* out;           /* [batch][256] last layer's outputs, or NULL           */
+  void* xt;             /* bf16 [64][batch] transposed inputs (training; rows 6..63 stay zero) */
+  float* loss;          /* [1] += squared error over the 200 outputs (training; caller clears) */
+  int32_t* err;         /* [1] set to 1 if a completion wait timed out          */
+  float loss_scale;     /* loss gradient 2 (out - target) * loss_scale          */
+  int32_t batch;        /* multiple of 128                                      */
+  int32_t training;
+  int32_t target_ld;    /* elements between target rows (>= 200)               */
+} mcl_mlp_args;
+int mcl_mlp_fused(const mcl_mlp_args* args, void* stream);
+
+/* Several plain GEMMs C = A B^T (fp32 output, as mcl_gemm_nt_tc with
+ * MCL_EPI_F32) in ONE launch, each with its K split over a thread-block
+ * cluster of `splits` CTAs (1, 2, 4 or 8; K a multiple of 64 * splits, and
+ * at least two 64-wide slabs per CTA when split): the surrogate's weight
+ * gradients of all layers at once.  Up to 8 GEMMs. */
+typedef struct mcl_gemm_desc {
+  const void* A;  /* bf16 [M][lda] */
+  const void* B;  /* bf16 [N][ldb] */
+  float* C;       /* fp32 [M][ldc] */
+  int32_t M, N, K, lda, ldb, ldc;
+} mcl_gemm_desc;
+int mcl_gemm_nt_tc_grouped(const mcl_gemm_desc* gemms, int32_t n, int32_t splits, int32_t* err, void* stream);
 /* dZ = dY * gelu'(Z) (or dY when gelu_on == 0) as bf16 in [M][N] and [N][M];
  * db[n] += sum_m dZ[m][n] (db must be cleared by the caller). */
 int mcl_act_backward(int32_t M, int32_t N, const float* dY, int32_t lddy, const float* Z, int32_t ldz,

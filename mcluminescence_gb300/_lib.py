@@ -92,6 +92,26 @@ class AdamTensor(C.Structure):
                 ("W", C.c_void_p), ("Wt", C.c_void_p), ("rows", C.c_int32), ("cols", C.c_int32)]
 
 
+class MlpLayer(C.Structure):
+    """mcl_mlp_layer (include/mclum.h)."""
+    _fields_ = [("W", C.c_void_p), ("Wt", C.c_void_p), ("bias", C.c_void_p), ("grad_b", C.c_void_p),
+                ("dZt", C.c_void_p), ("gelu_grad", C.c_void_p), ("Yt", C.c_void_p)]
+
+
+class MlpArgs(C.Structure):
+    """mcl_mlp_args (include/mclum.h)."""
+    _fields_ = [("layer", MlpLayer * 5), ("x", C.c_void_p), ("idx", C.c_void_p), ("target", C.c_void_p),
+                ("out", C.c_void_p), ("xt", C.c_void_p), ("loss", C.c_void_p), ("err", C.c_void_p),
+                ("loss_scale", C.c_float), ("batch", C.c_int32), ("training", C.c_int32),
+                ("target_ld", C.c_int32)]
+
+
+class GemmDesc(C.Structure):
+    """mcl_gemm_desc (include/mclum.h)."""
+    _fields_ = [("A", C.c_void_p), ("B", C.c_void_p), ("C", C.c_void_p), ("M", C.c_int32), ("N", C.c_int32),
+                ("K", C.c_int32), ("lda", C.c_int32), ("ldb", C.c_int32), ("ldc", C.c_int32)]
+
+
 class MclError(RuntimeError):
     """A negative status.  ``detail`` appends the library's last error text
     (set by the entry point that just returned ``code``); device status words
@@ -136,6 +156,8 @@ def _declare(lib):
         "mcl_gemm_nt": (C.c_int, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32, vp]),
         "mcl_gemm_nt_tc": (C.c_int, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32, vp, vp]),
         "mcl_act_backward": (C.c_int, [i32, i32, vp, i32, vp, i32, i32, vp, i32, vp, i32, vp, vp]),
+        "mcl_mlp_fused": (C.c_int, [C.POINTER(MlpArgs), vp]),
+        "mcl_gemm_nt_tc_grouped": (C.c_int, [vp, i32, i32, vp, vp]),
         "mcl_mse_loss": (C.c_int, [i32, i32, i32, vp, i32, vp, i32, C.c_float, vp, i32, vp, vp]),
         "mcl_adam": (C.c_int, [i32, i32, vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
                                i32, vp, vp, vp]),
@@ -168,7 +190,7 @@ EXPORTS = (
     "mcl_gemm_nt", "mcl_gemm_nt_tc", "mcl_act_backward", "mcl_mse_loss", "mcl_adam", "mcl_f32_to_bf16",
     "mcl_glow_extent", "mcl_glow_hist", "mcl_running_mean", "mcl_adam_multi", "mcl_adam_multi_dev",
     "mcl_k_region_bytes", "mcl_k_arrays_fit_smem", "mcl_k_box_nearest", "mcl_k_box_waits",
-    "mcl_k_box_distances",
+    "mcl_k_box_distances", "mcl_mlp_fused", "mcl_gemm_nt_tc_grouped",
 )
 
 

@@ -16,6 +16,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace mcl {
 namespace {
@@ -23,14 +24,6 @@ namespace {
 constexpr int BM = 64, BN = 64, BK = 32;
 constexpr int PAD = 8;              // bf16 elements of row padding (bank spread)
 constexpr int LDS = BK + PAD;       // shared-memory row stride (elements)
-
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-
-__device__ __forceinline__ float gelu_grad(float z) {
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
-  return cdf + z * pdf;
-}
 
 __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* p) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
@@ -274,83 +267,11 @@ __global__ void __launch_bounds__(256) f32_to_bf16(int64_t n, const float* __res
 // ---------------------------------------------------------------------------
 namespace tc {
 
+using namespace ::mcl::tcg;
+
 constexpr int kM = 128;   // rows per CTA (one tcgen05.mma M)
 constexpr int kKS = 64;   // K elements staged per slab
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Shared-memory matrix descriptor: start address, leading (K) and stride
-// (M/N) byte offsets >> 4, descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-  for (int i = 0; i < (1 << 20); ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Start copying rows [m0, m0 + 128) of A and [n0, n0 + NT) of B (k-contiguous
 // bf16) x K slab [k0, k0 + 64) into the core-matrix layout at shared
@@ -388,12 +309,13 @@ constexpr int smem_bytes() {
 // distributed shared memory and every CTA sums 128/gridDim.z of the rows over
 // the cluster in rank order (deterministic).  Only the plain fp32 epilogue
 // uses it (the weight gradients, whose K is the batch).
+// One CTA's tile (tile_m, tile_n) of C, K range split `split` of `splits`.
 template <int EPI, int NT>
-__global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
-                                                  const __nv_bfloat16* __restrict__ B, int ldb,
-                                                  const float* __restrict__ bias, float* __restrict__ C, int ldc,
-                                                  __nv_bfloat16* __restrict__ Y, int ldy,
-                                                  __nv_bfloat16* __restrict__ Yt, int ldyt, int32_t* err) {
+__device__ __forceinline__ void gemm_tile(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+                                          const __nv_bfloat16* __restrict__ B, int ldb,
+                                          const float* __restrict__ bias, float* __restrict__ C, int ldc,
+                                          __nv_bfloat16* __restrict__ Y, int ldy, __nv_bfloat16* __restrict__ Yt,
+                                          int ldyt, int32_t* err, int tile_m, int tile_n, int split, int splits) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[kStages];
   __shared__ uint32_t tmem_slot;
@@ -402,9 +324,8 @@ __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __n
   auto slabA = [&](int q) { return sbase + q * kStageA; };
   auto slabB = [&](int q) { return sbase + kStages * kStageA + q * NT * kKS * 2; };
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.y * kM, n0 = blockIdx.x * NT;
-  const int splits = gridDim.z;
-  const int kper = K / splits, kbeg = blockIdx.z * kper, nk = kper / kKS;
+  const int m0 = tile_m * kM, n0 = tile_n * NT;
+  const int kper = K / splits, kbeg = split * kper, nk = kper / kKS;
   const uint32_t mb0 = smem_u32(&mbar[0]);  // barrier q at mb0 + 8 q; MMA j commits to barrier j % 3
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), NT);
   if (tid == 0) {
@@ -519,6 +440,33 @@ __global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __n
   if (warp == 0) tmem_dealloc(tmem, NT);
   (void)M;
   (void)N;
+}
+
+template <int EPI, int NT>
+__global__ void __launch_bounds__(128) gemm_nt_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+                                                  const __nv_bfloat16* __restrict__ B, int ldb,
+                                                  const float* __restrict__ bias, float* __restrict__ C, int ldc,
+                                                  __nv_bfloat16* __restrict__ Y, int ldy,
+                                                  __nv_bfloat16* __restrict__ Yt, int ldyt, int32_t* err) {
+  gemm_tile<EPI, NT>(M, N, K, A, lda, B, ldb, bias, C, ldc, Y, ldy, Yt, ldyt, err, blockIdx.y, blockIdx.x, blockIdx.z,
+                     gridDim.z);
+}
+
+// Several independent plain (fp32 output) GEMMs in one launch: blockIdx.z =
+// gemm * splits + split, the split-K cluster running along z inside one
+// GEMM.  CTAs whose tile lies outside their GEMM leave at once; a cluster
+// shares its (x, y), so its CTAs leave together.
+struct Grouped {
+  mcl_gemm_desc g[8];
+};
+
+__global__ void __launch_bounds__(128) gemm_nt_tc_grouped(const __grid_constant__ Grouped G, int splits,
+                                                          int32_t* err) {
+  const mcl_gemm_desc& d = G.g[blockIdx.z / splits];
+  if ((int)blockIdx.x * 64 >= d.N || (int)blockIdx.y * kM >= d.M) return;
+  gemm_tile<EPI_F32, 64>(d.M, d.N, d.K, reinterpret_cast<const __nv_bfloat16*>(d.A), d.lda,
+                         reinterpret_cast<const __nv_bfloat16*>(d.B), d.ldb, nullptr, d.C, d.ldc, nullptr, 0, nullptr,
+                         0, err, blockIdx.y, blockIdx.x, blockIdx.z % splits, splits);
 }
 
 }  // namespace tc
@@ -668,6 +616,41 @@ int launch_tc(dim3 grid, int splits, int M, int N, int K, const __nv_bfloat16* a
 }
 }  // namespace
 }  // namespace mcl
+
+extern "C" int mcl_gemm_nt_tc_grouped(const mcl_gemm_desc* gemms, int32_t n, int32_t splits, int32_t* err,
+                                      void* stream) {
+  if (!gemms || n < 1 || n > 8 || !err || (splits != 1 && splits != 2 && splits != 4 && splits != 8))
+    return MCL_EINVAL;
+  tc::Grouped G;
+  int gx = 0, gy = 0;
+  for (int i = 0; i < n; ++i) {
+    const mcl_gemm_desc& d = gemms[i];
+    if (d.M <= 0 || d.N <= 0 || d.K <= 0 || d.M % tc::kM || d.N % 64 || d.K % (tc::kKS * splits)) return MCL_EINVAL;
+    if (splits > 1 && d.K / splits < 2 * tc::kKS) return MCL_EINVAL;
+    if (!d.A || !d.B || !d.C || d.lda < d.K || d.ldb < d.K || d.ldc < d.N || (d.lda % 8) || (d.ldb % 8))
+      return MCL_EINVAL;
+    if (((uintptr_t)d.A | (uintptr_t)d.B) & 15) return MCL_EINVAL;
+    G.g[i] = d;
+    gx = std::max(gx, d.N / 64);
+    gy = std::max(gy, d.M / tc::kM);
+  }
+  constexpr int smem = tc::smem_bytes<64>();
+  MCL_CUDA_TRY(cudaFuncSetAttribute(tc::gemm_nt_tc_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)gx, (unsigned)gy, (unsigned)(n * splits));
+  cfg.blockDim = dim3(128, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = reinterpret_cast<cudaStream_t>(stream);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 1;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = (unsigned)splits;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  MCL_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc::gemm_nt_tc_grouped, G, (int)splits, err));
+  return MCL_OK;
+}
 
 extern "C" int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                               const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,

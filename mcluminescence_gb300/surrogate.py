@@ -191,6 +191,19 @@ class SurrogateMLP:
         self.use_tcgen05 = True
         self.training = True      # False: forward only (no transposed copies for backward)
         self.step_count = 0
+        # the fused path (mcl_mlp_fused): one launch per forward pass, or per
+        # forward + loss + input-gradient chain in training; then one grouped
+        # launch for the weight gradients
+        self.use_fused = batch % 128 == 0
+        self.x_f32 = f32(B, 6)
+        self.G = [f32(B, n) for n in self.outs[:-1]]     # GELU'(pre-activation) per hidden layer
+        self.gb_all = f32(sum(self.outs))                  # the bias gradients, cleared together
+        o = 0
+        for L, n in zip(self.layers, self.outs):
+            L.gb = self.gb_all[o:o + n]
+            o += n
+        self._fused = {}
+        self._dw = None
 
     # -- plumbing -------------------------------------------------------------
     def _s(self):
@@ -219,6 +232,9 @@ class SurrogateMLP:
     def set_inputs(self, x_std: "torch.Tensor") -> None:
         """x_std: float tensor [B][6] of standardized parameters (device)."""
         t = self.torch
+        if self.use_fused:
+            self.x_f32.copy_(x_std)
+            return
         x = t.zeros(self.B, IN_PAD, dtype=t.bfloat16, device=self.dev)
         x[:, :6] = x_std.to(t.bfloat16)
         self.x0.copy_(x)
@@ -228,8 +244,67 @@ class SurrogateMLP:
     def set_targets(self, y: "torch.Tensor") -> None:
         self.target[:, :DIMS[-1]].copy_(y)
 
+    # -- fused passes -----------------------------------------------------------
+    def _fused_args(self, training: bool, x, idx, target, target_ld: int) -> _lib.MlpArgs:
+        key = (training, x.data_ptr(), idx.data_ptr() if idx is not None else 0, target.data_ptr(), target_ld)
+        a = self._fused.get(key)
+        if a is not None:
+            return a
+        a = _lib.MlpArgs()
+        for l, L in enumerate(self.layers):
+            d = a.layer[l]
+            d.W, d.Wt, d.bias = L.Wb.data_ptr(), L.Wt.data_ptr(), L.b.data_ptr()
+            if training:
+                d.grad_b, d.dZt = L.gb.data_ptr(), self.dZt[l].data_ptr()
+                if l < len(self.layers) - 1:
+                    d.gelu_grad, d.Yt = self.G[l].data_ptr(), self.Yt[l].data_ptr()
+        a.x = x.data_ptr()
+        a.idx = idx.data_ptr() if idx is not None else None
+        a.target = target.data_ptr()
+        a.out = self.Z[-1].data_ptr()
+        a.xt = self.x0t.data_ptr()
+        a.loss = self.loss.data_ptr()
+        a.err = self.tc_err.data_ptr()
+        a.loss_scale = 1.0 / (self.B * DIMS[-1])
+        a.batch = self.B
+        a.training = 1 if training else 0
+        a.target_ld = target_ld
+        self._fused[key] = a
+        return a
+
+    def fused_pass(self, x, target=None, idx=None, target_ld: int = OUT_PAD) -> None:
+        """One mcl_mlp_fused launch on inputs ``x`` (device fp32 [*][6],
+        standardized) and, in training, ``target`` (device fp32 [*][target_ld]);
+        ``idx`` (device int64 [B]) picks the rows, else rows 0..B-1.  Training
+        clears the bias gradients and the loss first."""
+        training = self.training and target is not None
+        if training:
+            self.gb_all.zero_()
+            self.loss.zero_()
+        a = self._fused_args(training, x, idx, target if target is not None else x, target_ld)
+        _lib.check(self.lib.mcl_mlp_fused(C.byref(a), self._s()), "mcl_mlp_fused")
+
+    def weight_grads(self) -> None:
+        """All layers' weight gradients dW_l = dZ_l^T X_l in one grouped
+        split-K launch (after a training fused_pass)."""
+        if self._dw is None:
+            descs = []
+            for l, L in enumerate(self.layers):
+                n, k = self.outs[l], self.ins[l]
+                Xt = self.Yt[l - 1] if l > 0 else self.x0t
+                descs.append(_lib.GemmDesc(self.dZt[l].data_ptr(), Xt.data_ptr(), L.gW.data_ptr(),
+                                           n, k, self.B, self.B, self.B, k))
+            self._dw = (_lib.GemmDesc * len(descs))(*descs)
+        splits = 8 if self.B % (64 * 8) == 0 else 1
+        _lib.check(self.lib.mcl_gemm_nt_tc_grouped(C.cast(self._dw, C.c_void_p), len(self._dw), splits,
+                                                   self._p(self.tc_err), self._s()), "mcl_gemm_nt_tc_grouped")
+
     # -- passes ---------------------------------------------------------------
     def forward(self) -> "torch.Tensor":
+        if self.use_fused:
+            # training: forward, loss and the input-gradient chain in one launch
+            self.fused_pass(self.x_f32, self.target if self.training else None)
+            return self.Z[-1][:, :DIMS[-1]]
         B = self.B
         A, lda = self.x0, IN_PAD
         for l, L in enumerate(self.layers):
@@ -243,7 +318,15 @@ class SurrogateMLP:
         return self.Z[-1][:, :DIMS[-1]]
 
     def backward(self, want_input_grad: bool = False) -> None:
-        """Gradients of the mean squared error (over batch and 200 bins)."""
+        """Gradients of the mean squared error (over batch and 200 bins).  On
+        the fused path forward() already ran the loss and the input-gradient
+        chain, so only the weight gradients remain (the input gradient needs
+        the layer-by-layer path: set ``use_fused = False`` before forward)."""
+        if self.use_fused:
+            if want_input_grad:
+                raise ValueError("input gradients need use_fused = False before forward()")
+            self.weight_grads()
+            return
         B = self.B
         self.loss.zero_()
         _lib.check(self.lib.mcl_mse_loss(B, OUT_PAD, DIMS[-1], self._p(self.Z[-1]), OUT_PAD,
@@ -317,6 +400,7 @@ class SurrogateMLP:
         m = SurrogateMLP(batch=b, seed=0, device=str(self.dev))
         m.load_state_dict(self.state_dict())
         m.training = False
+        m.use_fused = self.use_fused
         return m
 
     def input_grad(self) -> "torch.Tensor":
@@ -386,11 +470,20 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
            for k in range(steps)]
     hist = []
 
-    def body(k):
-        model.set_inputs(X.index_select(0, idx))
-        model.set_targets(Y.index_select(0, idx))
+    def step_on(ix):
+        """One forward/backward pass on rows ``ix`` of the dataset."""
+        if model.use_fused:
+            # the fused kernel gathers its rows itself: no copies of the batch
+            model.fused_pass(X, Y, idx=ix, target_ld=Y.shape[1])
+            model.weight_grads()
+            return
+        model.set_inputs(X.index_select(0, ix))
+        model.set_targets(Y.index_select(0, ix))
         model.forward()
         model.backward()
+
+    def body(k):
+        step_on(idx)
         model.adam_step(lr=lrs[k])
 
     if not use_graph:
@@ -411,18 +504,12 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
     s = t.cuda.Stream()
     s.wait_stream(t.cuda.current_stream())
     with t.cuda.stream(s):   # one eager forward/backward before the capture
-        model.set_inputs(X.index_select(0, idxs[0]))
-        model.set_targets(Y.index_select(0, idxs[0]))
-        model.forward()
-        model.backward()
+        step_on(idxs[0])
     t.cuda.current_stream().wait_stream(s)
     g = t.cuda.CUDAGraph()
     with t.cuda.graph(g):
         for j in range(G):
-            model.set_inputs(X.index_select(0, idxs[j]))
-            model.set_targets(Y.index_select(0, idxs[j]))
-            model.forward()
-            model.backward()
+            step_on(idxs[j])
             model.adam_step_dev(lr_cur[j:].data_ptr(), base.data_ptr(), j + 1)
     k = 0
     while k + G <= steps:

@@ -36,12 +36,17 @@ def test_gemm_nt_matches_torch(epi, M, N, K):
         assert torch.equal(Yt, gy.t().contiguous())
 
 
-@pytest.mark.parametrize("tcgen05", [True, False])
-def test_gradients_match_float64_reference(tcgen05):
+@pytest.mark.parametrize("path", ["fused", "tcgen05", "mma_sync"])
+def test_gradients_match_float64_reference(path):
+    """Forward, loss and every parameter gradient against a float64 autograd
+    reference of the same network (bf16 weights, inputs and hidden
+    activations): the fused whole-network kernel, the layer-by-layer tcgen05
+    GEMMs and the mma.sync GEMMs."""
     import torch
     from mcluminescence_gb300 import surrogate as S
     m = S.SurrogateMLP(batch=256, seed=3)
-    m.use_tcgen05 = tcgen05
+    m.use_fused = path == "fused"
+    m.use_tcgen05 = path != "mma_sync"
     rng = np.random.default_rng(0)
     x = S.standardize(S.sample_params(256, rng))
     y = rng.normal(-2.0, 0.5, (256, 200)).astype(np.float32)
@@ -142,3 +147,49 @@ def test_gemm_tcgen05_matches_torch(epi, M, N, K):
     if epi == 2:
         assert torch.equal(Yt, Y.t().contiguous())
         assert (Y.float() - torch.nn.functional.gelu(Cm).to(torch.bfloat16).float()).abs().max() == 0
+
+
+def _train_pass(m, x, y):
+    import torch
+    m.set_inputs(torch.tensor(x, dtype=torch.float32, device="cuda"))
+    m.set_targets(torch.tensor(y, device="cuda"))
+    out = m.forward().float().clone()
+    m.backward()
+    torch.cuda.synchronize()
+    m.check_errors()
+    return (out, float(m.loss.item()), [L.gW.clone() for L in m.layers], [L.gb.clone() for L in m.layers])
+
+
+def test_fused_step_matches_layer_by_layer():
+    """At batch 4,096 (32 tiles; weight gradients split over 8-CTA clusters)
+    the fused launch and the grouped weight-gradient launch give what the
+    layer-by-layer tcgen05 kernels give: same GEMMs, same bf16 roundings, the
+    sums in another order."""
+    import torch
+    from mcluminescence_gb300 import surrogate as S
+    B = 4096
+    rng = np.random.default_rng(5)
+    x = S.standardize(S.sample_params(B, rng))
+    y = rng.normal(-2.0, 0.5, (B, 200)).astype(np.float32)
+    fused = S.SurrogateMLP(batch=B, seed=7)
+    plain = S.SurrogateMLP(batch=B, seed=7)
+    plain.use_fused = False
+    a = _train_pass(fused, x, y)
+    b = _train_pass(plain, x, y)
+    torch.testing.assert_close(a[0], b[0], rtol=1e-3, atol=1e-3)
+    assert abs(a[1] - b[1]) <= 1e-4 * abs(b[1])
+    for ga, gb_ in zip(a[2] + a[3], b[2] + b[3]):
+        assert float(torch.linalg.norm(ga - gb_)) <= 1e-3 * float(torch.linalg.norm(gb_)) + 1e-12
+
+
+def test_fused_inference_matches_layer_by_layer():
+    import torch
+    from mcluminescence_gb300 import surrogate as S
+    m = S.SurrogateMLP(batch=512, seed=9)
+    inf_f = m.inference_copy(1024)
+    inf_p = m.inference_copy(1024)
+    inf_p.use_fused = False
+    p = torch.tensor(S.sample_params(1000, np.random.default_rng(2)), dtype=torch.float32, device="cuda")
+    a, b = S.predict_t(inf_f, p), S.predict_t(inf_p, p)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(a, b, rtol=1e-3, atol=1e-3)
