@@ -66,6 +66,17 @@ def parse():
     return p.parse_args()
 
 
+def measured_peaks() -> dict:
+    """The machine's measured peaks (MEASURED_PEAKS.json next to this file),
+    else the figures recorded when it was last read."""
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {k: float(d[k]) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6797.2, "bf16_tflops": 1926.0, "bf16_tflops_sustained": 1735.4}
+
+
 def measured_hbm_gbs() -> float:
     """Copy bandwidth measured on the GB300s (MEASURED_PEAKS.json next
     to this file), else the same figure recorded when the file was read."""
@@ -518,6 +529,33 @@ def fitting_bench(a, rank):
     hist = S.train(m, P, Cn, steps=8000, log_every=2000)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    # device time of one training step (graph-replayed) and of one forward
+    # pass over the fitting DE's 32,768 candidates, with their tensor roofline
+    peaks = measured_peaks()
+    step_us = S.time_training_steps(m, P[:200000], Cn[:200000])
+    step_flop = S.flops_per_step(m)
+    inf = m.inference_copy(32768)
+    xs = torch.tensor(S.sample_params(32768, np.random.default_rng(3)), dtype=torch.float32, device="cuda")
+    S.predict_t(inf, xs)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        S.predict_t(inf, xs)
+    e1.record()
+    e1.synchronize()
+    inf_us = e0.elapsed_time(e1) * 1e3 / 10
+    inf_flop = sum(2.0 * 32768 * k * n for k, n in zip(inf.ins, inf.outs))
+    mlp_roof = {
+        "bound": "tensor", "unit": "TFLOP/s",
+        "train_step_us": step_us, "train_step_flop": step_flop,
+        "achieved": step_flop / (step_us * 1e-6) / 1e12, "peak": peaks["bf16_tflops_sustained"],
+        "frac": step_flop / (step_us * 1e-6) / 1e12 / peaks["bf16_tflops_sustained"],
+        "peak_basis": "bf16_tflops_sustained of measured (a training run is a long loop)",
+        "forward_32768_us": inf_us,
+        "forward_32768_tflops": inf_flop / (inf_us * 1e-6) / 1e12,
+        "forward_32768_frac_of_burst": inf_flop / (inf_us * 1e-6) / 1e12 / peaks["bf16_tflops"],
+        "kernels_per_step": {"mlp_fused": 1, "gemm_nt_tc_grouped": 1, "adam_multi": 1},
+    }
     Ph, Ch = S.generate_dataset(10000, seed=a.seed + 12, id0=10 ** 7)
     pred = S.target_to_curve(S.predict(m, Ph))
     big = Ch > 20
@@ -536,6 +574,7 @@ def fitting_bench(a, rank):
         "surrogate": {"train_curves": len(P), "datagen_s": t1 - t0, "train_steps": 8000,
                       "train_s": t2 - t1, "loss_history": hist,
                       "heldout_curves": len(Ph), "heldout_rms_err_over_mc_se": err_over_se},
+        "mlp_roofline": mlp_roof,
         "surrogate_mc": sur.as_dict(), "plain_mc": plain.as_dict(),
         "fits_per_s_ratio": sur.fits_per_s / plain.fits_per_s if plain.fits_per_s else None,
         "mc_trials_per_fit_ratio": (plain.mc_trials / plain.n_fits) / (sur.mc_trials / sur.n_fits),

@@ -358,7 +358,8 @@ typedef struct mcl_mlp_layer {
   const float* bias;    /* [256]                                               */
   float* grad_b;        /* [256] += bias gradient (training; caller clears)    */
   void* dZt;            /* bf16 [256][batch] d loss / d pre-activation, transposed (training) */
-  float* gelu_grad;     /* [batch][256] GELU' of the pre-activation (training, layers 0..3) */
+  float* gelu_grad;     /* batch x 256 floats: GELU' of the pre-activation, in a layout
+                           private to the kernel (training scratch, layers 0..3)  */
   void* Yt;             /* bf16 [256][batch] activation, transposed (training, layers 0..3) */
 } mcl_mlp_layer;
 

@@ -531,6 +531,59 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
     return hist
 
 
+def flops_per_step(model: SurrogateMLP) -> float:
+    """Multiply-add FLOPs of one training step: the forward GEMMs, the
+    weight-gradient GEMMs and the input-gradient GEMMs of layers 1..4."""
+    fwd = sum(2.0 * model.B * k * n for k, n in zip(model.ins, model.outs))
+    dx = sum(2.0 * model.B * k * n for k, n in zip(model.ins[1:], model.outs[1:]))
+    return 2.0 * fwd + dx
+
+
+def time_training_steps(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, graph_steps: int = 25,
+                        replays: int = 8, seed: int = 0, n_traps: int = N_TRAPS) -> float:
+    """Device time of one training step (forward, loss, backward, Adam on a
+    random mini-batch): ``graph_steps`` steps captured in one CUDA graph,
+    replayed ``replays`` times between CUDA events.  Returns microseconds per
+    step.  The model's weights keep training while it is timed."""
+    t = model.torch
+    X = t.tensor(standardize(params), dtype=t.float32, device=model.dev)
+    Y = t.tensor(curve_to_target(counts, n_traps), dtype=t.float32, device=model.dev)
+    gen = t.Generator(device=model.dev).manual_seed(seed)
+    idxs = t.randint(0, X.shape[0], (graph_steps, model.B), generator=gen, device=model.dev)
+    lr = t.full((graph_steps,), 1e-4, dtype=t.float32, device=model.dev)
+    base = t.full((1,), model.step_count, dtype=t.int32, device=model.dev)
+
+    def step(j):
+        if model.use_fused:
+            model.fused_pass(X, Y, idx=idxs[j], target_ld=Y.shape[1])
+            model.weight_grads()
+        else:
+            model.set_inputs(X.index_select(0, idxs[j]))
+            model.set_targets(Y.index_select(0, idxs[j]))
+            model.forward()
+            model.backward()
+        model.adam_step_dev(lr[j:].data_ptr(), base.data_ptr(), j + 1)
+
+    s = t.cuda.Stream()
+    s.wait_stream(t.cuda.current_stream())
+    with t.cuda.stream(s):
+        step(0)
+    t.cuda.current_stream().wait_stream(s)
+    g = t.cuda.CUDAGraph()
+    with t.cuda.graph(g):
+        for j in range(graph_steps):
+            step(j)
+    g.replay()
+    e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(replays):
+        g.replay()
+    e1.record()
+    e1.synchronize()
+    model.check_errors()
+    return e0.elapsed_time(e1) * 1e3 / (replays * graph_steps)
+
+
 def predict(model: SurrogateMLP, params: np.ndarray) -> np.ndarray:
     """Predicted log curves [n][200] (float32, host)."""
     t = model.torch
