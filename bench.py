@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--ept", type=int, default=0)
     p.add_argument("--occupancy", type=int, default=0,
                    help="register-capped FP32 build (resident CTAs per SM it targets; 0 = default)")
+    p.add_argument("--bin-copies", type=int, default=1, help="copies of the bins per FP32 CTA (1, 2, 4)")
     p.add_argument("--sets", type=int, default=N_SETS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -193,11 +194,11 @@ def main():
     specs = schedule.batch_tl_iso(a.sets, seed=a.seed + 7919 * rank)
     for s in specs:
         s.set_id += rank * a.sets
-    block, ept, occ = a.block, a.ept, a.occupancy
-    if not block or not ept:
-        block, ept, occ = autotune.pick_bernoulli(specs, precision="fp32")
-    batch = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=block, ept=ept,
-                           want_alive=True, occupancy=occ)
+    shape = autotune.Shape(a.block, a.ept, a.occupancy, a.bin_copies)
+    if not shape.block or not shape.ept:
+        shape = autotune.pick_bernoulli(specs, precision="fp32")
+    block, ept, occ, copies = shape
+    batch = BernoulliBatch(specs, precision="fp32", seed=a.seed, want_alive=True, **shape._asdict())
     stream = torch.cuda.Stream()
     batch.capture(stream)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -242,12 +243,12 @@ def main():
     # ---- end to end through the public API (host specs in, host bins out) ----
     e2e = None
     if not a.no_e2e:
-        res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, occupancy=occ)
+        res = simulate_batch(specs, precision="fp32", seed=a.seed, **shape._asdict())
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(a.steps):
-            res = simulate_batch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, occupancy=occ)
+            res = simulate_batch(specs, precision="fp32", seed=a.seed, **shape._asdict())
         torch.cuda.synchronize()
         barrier()
         e2e_s = (time.perf_counter() - t0) / a.steps
@@ -285,6 +286,7 @@ def main():
                    "sets_per_gpu": a.sets, "traps_per_gpu": int(sum(s.n_slots for s in specs)),
                    "trials_per_step_per_gpu": int(trials), "precision": "fp32",
                    "rng": "philox4x32-10", "block": block, "ept": ept, "occupancy_build": occ,
+                   "bin_copies": copies,
                    "filling_path_built": not batch.no_fill, "n_items": batch.n_items,
                    "l2": "flushed between passes (256 MB write, untimed)",
                    "parallelism": f"replicas x{world} (independent sets, no collective)"},
@@ -330,9 +332,8 @@ def variants_bench(a, rank, specs_own):
         for prec in ("fp32", "fp64"):
             if name == "own_alpha" and prec == "fp32":
                 continue                      # the headline measurement
-            block, ept, occ = autotune.pick_bernoulli(specs, precision=prec)
-            b = BernoulliBatch(specs, precision=prec, seed=a.seed, block=block, ept=ept,
-                               want_alive=True, occupancy=occ)
+            shape = autotune.pick_bernoulli(specs, precision=prec)
+            b = BernoulliBatch(specs, precision=prec, seed=a.seed, want_alive=True, **shape._asdict())
             st = torch.cuda.Stream()
             b.capture(st)
             b.replay(st)
@@ -355,7 +356,7 @@ def variants_bench(a, rank, specs_own):
                 "alpha": "rho'^(-1/3) of each set" if name == "own_alpha" else 5.0,
                 "precision": prec, "sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": m,
                 "electron_steps_per_s": b.trials / (m / 1e3), "events_per_pass": int(b.result().lum.sum()),
-                "block": block, "ept": ept, "occupancy_build": occ}
+                **shape._asdict()}
             del b
     return out
 
@@ -400,9 +401,8 @@ def sequence_bench(a, rank):
     import torch
     from mcluminescence_gb300 import BernoulliBatch, autotune, schedule
     specs = schedule.batch_dose_fade_irsl(2048, seed=a.seed + 1 + 977 * rank)
-    block, ept, occ = autotune.pick_bernoulli(specs, precision="fp32")
-    b = BernoulliBatch(specs, precision="fp32", seed=a.seed, block=block, ept=ept, want_alive=True,
-                       occupancy=occ)
+    shape = autotune.pick_bernoulli(specs, precision="fp32")
+    b = BernoulliBatch(specs, precision="fp32", seed=a.seed, want_alive=True, **shape._asdict())
     st = torch.cuda.Stream()
     b.capture(st)
     for _ in range(2):
@@ -420,7 +420,7 @@ def sequence_bench(a, rank):
     ms = e0.elapsed_time(e1) / reps
     steps = [s.total_steps for s in specs]
     return {"sets": len(specs), "trials_per_pass": b.trials, "ms_per_pass": ms,
-            "block": block, "ept": ept, "occupancy_build": occ, "filling_path_built": not b.no_fill,
+            **shape._asdict(), "filling_path_built": not b.no_fill,
             "electron_steps_per_s": b.trials / (ms / 1e3), "steps_min": min(steps), "steps_max": max(steps),
             "events_per_pass": int(b.result().lum.sum())}
 

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MCL_ABI_VERSION 2
+#define MCL_ABI_VERSION 3
 
 /* ---- return / status codes ------------------------------------------- */
 #define MCL_OK 0
@@ -147,6 +147,13 @@ typedef struct mcl_b_args {
                               then uses its build without the filling path
                               (fewer registers), and a filling segment sets
                               MCL_EINVAL in the status word                   */
+  int32_t bin_copies;      /* FP32: copies of the set's bins each CTA keeps in
+                              shared memory (1, 2 or 4; 0 = 1): warp w adds its
+                              events to copy w % bin_copies, which spreads the
+                              shared-memory atomics of hot bins; the copies are
+                              summed when the CTA flushes.  Results do not
+                              depend on it.  FP64 keeps one copy.            */
+  int32_t reserved;
 } mcl_b_args;
 
 /* ---- reference-kinetics (event-driven) mode ----------------------------- */

@@ -23,7 +23,7 @@ MCL_ENODEV = -5
 MCL_ENOHOLE = -6
 MCL_EOVERFLOW = -7
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 MCL_FP32 = 0
 MCL_FP64 = 1
@@ -56,6 +56,7 @@ class BArgs(C.Structure):
         ("slots_per_item", C.c_int32), ("max_bins", C.c_int32), ("precision", C.c_int32),
         ("rng", C.c_int32), ("block", C.c_int32), ("ept", C.c_int32), ("grid", C.c_int32),
         ("zero_outputs", C.c_int32), ("occupancy", C.c_int32), ("no_fill", C.c_int32),
+        ("bin_copies", C.c_int32), ("reserved", C.c_int32),
     ]
 
 

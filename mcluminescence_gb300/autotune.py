@@ -3,15 +3,17 @@
 Times each (threads per CTA, traps per thread, register-capped build)
 candidate with CUDA events (best of three passes) on a deterministic sample
 of the batch (about 512 evenly strided sets, so the ragged size and step mix
-is kept) and caches the winner per (device, precision, shape bucket, with or
-without filling segments) in a JSON file next to the library.
+is kept), then the bins-per-CTA knob (how many copies of its sets' bins a CTA
+keeps in shared memory) on the winning shape, and caches the winner per
+(device, precision, shape bucket, with or without filling segments) in a JSON
+file next to the library.
 """
 from __future__ import annotations
 
 import json
 import math
 import os
-from typing import Sequence, Tuple
+from typing import NamedTuple, Sequence
 
 from . import build as _build
 from .schedule import SetSpec
@@ -21,7 +23,16 @@ CANDIDATES = {
              (256, 8, 2), (128, 8, 4), (256, 4, 3), (128, 4, 6), (256, 2, 4), (128, 2, 8)],
     "fp64": [(256, 1, 0), (256, 2, 0)],
 }
+BIN_COPIES = (1, 2, 4)
 CACHE = os.path.join(_build.LIBDIR, "autotune.json")
+
+
+class Shape(NamedTuple):
+    """Launch shape of the Bernoulli kernel; ``BernoulliBatch(**shape._asdict())``."""
+    block: int
+    ept: int
+    occupancy: int = 0
+    bin_copies: int = 1
 
 
 def _no_fill(specs: Sequence[SetSpec]) -> bool:
@@ -46,11 +57,11 @@ def _load():
         return {}
 
 
-def time_shape(specs, precision, block, ept, occupancy=0, reps=3) -> float:
+def time_shape(specs, precision, block, ept, occupancy=0, reps=3, bin_copies=1) -> float:
     import torch
     from .batch import BernoulliBatch
     b = BernoulliBatch(specs, precision=precision, seed=1, block=block, ept=ept, want_alive=True,
-                       occupancy=occupancy)
+                       occupancy=occupancy, bin_copies=bin_copies)
     s = torch.cuda.Stream()
     b.capture(s)
     b.replay(s)
@@ -66,12 +77,12 @@ def time_shape(specs, precision, block, ept, occupancy=0, reps=3) -> float:
 
 
 def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
-                   use_cache: bool = True) -> Tuple[int, int, int]:
-    """(block, ept, occupancy) of the fastest candidate for this batch shape."""
+                   use_cache: bool = True) -> Shape:
+    """The fastest launch shape for this batch shape."""
     key = _bucket(specs, precision)
     cache = _load() if use_cache else {}
-    if key in cache and len(cache[key]["best"]) == 3:
-        return tuple(cache[key]["best"])
+    if key in cache and len(cache[key]["best"]) == 4:
+        return Shape(*cache[key]["best"])
     # about 512 sets: enough work items per CTA that the launch's tail does
     # not decide the ranking
     sample = list(specs[::max(1, len(specs) // 512)]) or list(specs)
@@ -83,9 +94,18 @@ def pick_bernoulli(specs: Sequence[SetSpec], precision: str = "fp32",
     times = {}
     for blk, ept, occ in cands:
         times[(blk, ept, occ)] = time_shape(sample, precision, blk, ept, occ)
-    best = min(times, key=times.get)
+    blk, ept, occ = min(times, key=times.get)
+    ms = {f"{b}x{e}/{o}": t for (b, e, o), t in times.items()}
+    copies, t_best = 1, times[(blk, ept, occ)]
+    if precision == "fp32":
+        for c in BIN_COPIES[1:]:
+            t = time_shape(sample, precision, blk, ept, occ, bin_copies=c)
+            ms[f"{blk}x{ept}/{occ}/bins{c}"] = t
+            if t < t_best:
+                copies, t_best = c, t
+    best = Shape(blk, ept, occ, copies)
     cache = _load()
-    cache[key] = {"best": list(best), "ms": {f"{b}x{e}/{o}": t for (b, e, o), t in times.items()}}
+    cache[key] = {"best": list(best), "ms": ms}
     try:  # write-then-rename: processes sharing the library never see a torn file
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
         tmp = f"{CACHE}.{os.getpid()}.tmp"

@@ -106,12 +106,16 @@ class BernoulliBatch:
                  rng: str = "philox", seed: int = 0, block: int = 256, ept: int = 4,
                  grid: int = 0, want_alive: bool = True, want_fates: bool = False,
                  uniforms: Optional[np.ndarray] = None, device: str = "cuda", packed=None,
-                 occupancy: int = 0):
+                 occupancy: int = 0, bin_copies: int = 1):
         """``specs`` (a list of SetSpec) or ``packed`` = (sets, segs, bin_offsets,
         slot_offsets, u_offsets) host arrays as returned by ``pack_host``.
         ``occupancy`` picks a register-capped FP32 build by the resident CTAs
         per SM it targets (ept 2: 4 at block 256, 8 at block 128; ept 4: 3 at
-        block 256, 6 at block 128); 0 is the default build."""
+        block 256, 6 at block 128); 0 is the default build.  ``bin_copies``
+        (1, 2 or 4) is how many copies of its set's bins each FP32 CTA keeps in
+        shared memory; results do not depend on it."""
+        if int(bin_copies) not in (1, 2, 4):
+            raise ValueError(f"bin_copies must be 1, 2 or 4, not {bin_copies}")
         torch = _torch()
         self.lib = _lib.load()
         self.specs = list(specs) if specs is not None else None
@@ -123,6 +127,7 @@ class BernoulliBatch:
             ept = 2
         self.block, self.ept, self.grid = int(block), int(ept), int(grid)
         self.occupancy = int(occupancy) if self.precision == _lib.MCL_FP32 else 0
+        self.bin_copies = int(bin_copies) if self.precision == _lib.MCL_FP32 else 1
         sets, segs, b_off, s_off, u_off = packed if packed is not None else pack_host(self.specs)
         self.bin_offsets, self.slot_offsets, self.u_offsets = b_off, s_off, u_off
         self.n_bins_total = int(b_off[-1])
@@ -182,7 +187,7 @@ class BernoulliBatch:
         a.n_sets, a.n_segs, a.n_items = len(self.host_sets), len(self.host_segs), self.n_items
         a.slots_per_item, a.max_bins = self.block * self.ept, self.max_bins
         a.precision, a.rng, a.block, a.ept, a.grid = self.precision, self.rng, self.block, self.ept, self.grid
-        a.occupancy, a.no_fill = self.occupancy, self.no_fill
+        a.occupancy, a.no_fill, a.bin_copies = self.occupancy, self.no_fill, self.bin_copies
         a.zero_outputs = zero_outputs
         return a
 

@@ -95,10 +95,15 @@ extern "C" int mcl_b_run(const mcl_b_args* args, void* stream) {
   KernelFn fn = pick_kernel(a);
   if (!fn) return MCL_EINVAL;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const size_t smem = mcl_b_smem_bytes(a.max_bins, a.precision, a.alive != nullptr);
+  int copies = a.bin_copies <= 0 ? 1 : a.bin_copies;
+  if (copies != 1 && copies != 2 && copies != 4) return MCL_EINVAL;
+  if (a.precision != MCL_FP32) copies = 1;
+  size_t smem = mcl_b_smem_bytes(a.max_bins, a.precision, a.alive != nullptr);
+  smem += (size_t)(copies - 1) * a.max_bins * sizeof(uint32_t);
   if (smem > 200 * 1024) return MCL_ECAPACITY;
   KParams P;
   P.a = a;
+  P.a.bin_copies = copies;
   const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
   for (int r = 0; r < 10; ++r) {
     P.ks0[r] = k0 + (uint32_t)r * kPhiloxW0;

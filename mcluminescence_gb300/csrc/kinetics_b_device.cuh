@@ -182,19 +182,23 @@ __device__ __forceinline__ void warp_flush(uint32_t v, uint32_t* dst) {
   }
 }
 
+// The CTA's bins: `copies` copies of the recombination counts, max_bins
+// apart, and one of the filled counts.
 template <int BLOCK>
-__device__ __forceinline__ void zero_bins(uint32_t* s_lum, uint32_t* s_alive, int n_bins) {
+__device__ __forceinline__ void zero_bins(uint32_t* s_lum, uint32_t* s_alive, int n_bins, int copies = 1,
+                                          int stride = 0) {
   for (int b = threadIdx.x; b < n_bins; b += BLOCK) {
-    s_lum[b] = 0;
+    for (int c = 0; c < copies; ++c) s_lum[c * stride + b] = 0;
     if (s_alive) s_alive[b] = 0;
   }
 }
 
 template <int BLOCK>
-__device__ __forceinline__ void flush_bins(const mcl_b_args& a, const mcl_set& st,
-                                           const uint32_t* s_lum, const uint32_t* s_alive) {
+__device__ __forceinline__ void flush_bins(const mcl_b_args& a, const mcl_set& st, const uint32_t* s_lum,
+                                           const uint32_t* s_alive, int copies = 1, int stride = 0) {
   for (int b = threadIdx.x; b < st.n_bins; b += BLOCK) {
-    const uint32_t v = s_lum[b];
+    uint32_t v = s_lum[b];
+    for (int c = 1; c < copies; ++c) v += s_lum[c * stride + b];
     if (v) atomicAdd(&a.lum[st.bin_offset + b], v);
     if (s_alive) {
       const uint32_t al = s_alive[b];
@@ -558,7 +562,9 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
   float* s_c = reinterpret_cast<float*>(smem);
   float* s_q = s_c + kChunk;
   uint32_t* s_lum = reinterpret_cast<uint32_t*>(s_q + kChunk);
-  uint32_t* s_alive = a.alive ? s_lum + a.max_bins : nullptr;
+  const int copies = a.bin_copies;  // 1, 2 or 4 (the launcher normalises it)
+  uint32_t* s_alive = a.alive ? s_lum + copies * a.max_bins : nullptr;
+  uint32_t* s_lum_w = s_lum + ((int)(threadIdx.x >> 5) % copies) * a.max_bins;  // this warp's copy
   __shared__ int s_item;
   __shared__ float s_bm[2 * kBlocksPerChunk];
 
@@ -577,7 +583,7 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
       continue;
     }
     const mcl_set st = a.sets[item.set];
-    zero_bins<BLOCK>(s_lum, s_alive, st.n_bins);
+    zero_bins<BLOCK>(s_lum, s_alive, st.n_bins, copies, a.max_bins);
 
     const float alpha = (float)st.alpha;
     SlotState<EPT> S;
@@ -601,18 +607,18 @@ __device__ __forceinline__ void kb_f32_body(const KParams& P) {
       const mcl_segment sg = a.segs[st.seg_begin + g];
       if (sg.fill_rate > 0.0) {
         if constexpr (FILLS)
-          segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum, s_alive, bbase, kglob,
+          segment_f32<BLOCK, EPT, true>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum_w, s_alive, bbase, kglob,
                                         alpha);
         else  // the caller promised no filling segment (mcl_b_args.no_fill)
           report(a.status, MCL_EINVAL);
       } else
-        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum, s_alive, bbase, kglob,
+        segment_f32<BLOCK, EPT, false>(P, st, sg, S, tab + kglob, s_c, s_q, s_bm, s_lum_w, s_alive, bbase, kglob,
                                        alpha);
       bbase += (uint32_t)((sg.n_steps + 7) >> 3);
       kglob += sg.n_steps;
     }
     __syncthreads();
-    flush_bins<BLOCK>(a, st, s_lum, s_alive);
+    flush_bins<BLOCK>(a, st, s_lum, s_alive, copies, a.max_bins);
     __syncthreads();
   }
 }

@@ -208,6 +208,33 @@ def test_fill_fade_irsl_sequence_fp32_fates():
     assert mism <= 2
 
 
+@pytest.mark.parametrize("block,ept,occ,copies", [(256, 4, 0, 2), (256, 4, 0, 4), (128, 8, 4, 4),
+                                                   (128, 2, 8, 2)])
+def test_fp32_bin_copies_invariance(block, ept, occ, copies):
+    """Keeping 2 or 4 copies of the bins per CTA changes only where the
+    shared-memory atomics land: bins, alive counts and fates are identical."""
+    specs = mixed_specs()
+    ref = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=block, ept=ept,
+                         occupancy=occ)
+    got = simulate_batch(specs, precision="fp32", seed=5, want_fates=True, block=block, ept=ept,
+                         occupancy=occ, bin_copies=copies)
+    assert np.array_equal(ref.lum, got.lum)
+    assert np.array_equal(ref.alive, got.alive)
+    assert np.array_equal(ref.fates, got.fates)
+
+
+def test_fp32_bin_copies_over_shared_memory_is_refused():
+    """12,000 bins: one copy (plus the filled counts) fits in shared memory,
+    four copies do not, and the launcher says so instead of launching."""
+    S = schedule
+    spec = S.SetSpec(n_slots=64, E=1.3, s=1e12, alpha=5.0, set_id=1,
+                     segments=[S.isothermal(150.0, 12000.0, 1.0, 1.0)]).finalize()
+    assert spec.n_bins == 12000
+    simulate_batch([spec], precision="fp32", seed=3)
+    with pytest.raises(Exception, match="too small"):
+        simulate_batch([spec], precision="fp32", seed=3, bin_copies=4)
+
+
 def test_fp32_unknown_register_capped_build_is_rejected():
     with pytest.raises(Exception, match="invalid argument|EINVAL|MCL_EINVAL"):
         simulate_batch(mixed_specs()[:2], precision="fp32", seed=5, block=256, ept=8, occupancy=3)

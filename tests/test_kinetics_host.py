@@ -83,3 +83,11 @@ def test_batches_without_filling_are_recognised():
     assert autotune._no_fill(tl) and not autotune._no_fill(dose)
     assert not (pack_host(tl)[1]["fill_rate"] > 0).any()
     assert (pack_host(dose)[1]["fill_rate"] > 0).any()
+
+
+def test_bin_copies_must_be_one_two_or_four():
+    import pytest
+    from mcluminescence_gb300 import BernoulliBatch, schedule
+    specs = [schedule.single_tl_set(alpha=5.0, n_slots=10, set_id=1)]
+    with pytest.raises(ValueError, match="bin_copies"):
+        BernoulliBatch(specs, bin_copies=3, device="cpu")
