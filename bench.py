@@ -299,7 +299,7 @@ def main():
     out["dose_fade_irsl"] = sequence_bench(a, rank)
     out["single_set_tl"] = single_set_bench(a, rank, world)
     if not a.no_k:
-        out["reference_kinetics"] = kinetics_k_bench(a, rank, world)
+        out["reference_kinetics"] = kinetics_k_bench(a, rank, world, clk.get("sm_mhz"))
     if not a.no_fit:
         out["fitting"] = fitting_bench(a, rank)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -436,7 +436,7 @@ def _esteps(res, params):
     return tot
 
 
-def kinetics_k_bench(a, rank, world):
+def kinetics_k_bench(a, rank, world, sm_mhz=None):
     """Event-driven (reference) kinetics: the reference's default TL12
     configuration through the drop-in simulate() (numpy's global stream, runs
     in order), and 1,216 independent TL12-size simulations in parallel
@@ -464,18 +464,26 @@ def kinetics_k_bench(a, rank, world):
     n_par = 8 * 152
     K.run_kinetics([p5] * 8, 20000, rng="philox", seed=1, want_events=False)
     torch.cuda.synchronize()
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     t0 = time.perf_counter()
-    rp, _ = K.run_kinetics([p5] * n_par, 20000, rng="philox", seed=a.seed, want_events=False)
+    rp, _ = K.run_kinetics([p5] * n_par, 20000, rng="philox", seed=a.seed, want_events=False, timing=ev)
     torch.cuda.synchronize()
     par_s = time.perf_counter() - t0
+    kern_s = ev[0].elapsed_time(ev[1]) / 1e3
     par_esteps = _esteps(rp, [p5] * n_par)
+    from mcluminescence_gb300 import roofline
+    props = torch.cuda.get_device_properties(0)
+    kk_roof = roofline.kk_issue(par_esteps, kern_s, sm_mhz, props.multi_processor_count)
     out = {"compat_tl12": {"config": "reference default (TL12 x basicTL12: 4 heating rates x 2 sims, "
                                      "2000 traps, 3455 centres)", "seconds": compat_s,
                            "steps": int(np.sum(res.n_steps)), "events": int(lum.sum()),
                            "electron_steps": compat_esteps, "electron_steps_per_s": compat_esteps / compat_s},
-           "parallel_tl12_rate5": {"sims": n_par, "seconds": par_s, "electron_steps": par_esteps,
+           "parallel_tl12_rate5": {"sims": n_par, "seconds": par_s, "kernel_seconds": kern_s,
+                                   "electron_steps": par_esteps,
                                    "electron_steps_per_s": par_esteps / par_s,
-                                   "events": int(rp.lum.sum())}}
+                                   "kernel_electron_steps_per_s": par_esteps / kern_s,
+                                   "events": int(rp.lum.sum()),
+                                   "roofline": kk_roof}}
     # the reference's own CPU time on two golden cases (recorded when the
     # fixtures were generated from the unmodified reference, one x86 core):
     # the same inputs through simulate() here, outputs checked bit for bit

@@ -346,11 +346,15 @@ int mcl_gemm_nt(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A
 int mcl_gemm_nt_tc(int32_t epilogue, int32_t M, int32_t N, int32_t K, const void* A, int32_t lda,
                    const void* B, int32_t ldb, const float* bias, float* C, int32_t ldc, void* Y,
                    int32_t ldy, void* Yt, int32_t ldyt, int32_t* err, void* stream);
-/* The whole network in one persistent launch: one CTA per 128-row tile of
- * the batch keeps the tile's activations in shared memory and its
- * accumulator in tensor memory from layer to layer (tcgen05 MMAs with
- * M 128, N 256, K 16), copying each layer's weights from L2 while the
- * previous layer's epilogue runs.  Forward: bias + GELU epilogues, the last
+/* The whole network in one persistent launch: a thread-block cluster of
+ * `split` CTAs (1, 2 or 4) per 128-row tile of the batch keeps the tile's
+ * activations in shared memory (each CTA a full copy, which the CTAs write
+ * into each other's shared memory) and its accumulator in tensor memory from
+ * layer to layer; CTA q computes output columns [q 256/split, (q+1)
+ * 256/split) of every layer (tcgen05 MMAs with M 128, N 256/split, K 16),
+ * copying its slice of the next weights from L2 while the current epilogue
+ * runs.  split 0 lets the library pick the one with the fewest waves for
+ * this batch on this device.  Forward: bias + GELU epilogues, the last
  * layer's outputs to `out`.  Training adds, in the same launch and per
  * tile, the loss and its gradient (mcl_mse_loss's), then the input-gradient
  * chain dY_{l-1} = dZ_l W_l with dZ = dY * GELU'(pre-activation) fused into
@@ -383,6 +387,8 @@ typedef struct mcl_mlp_args {
   int32_t batch;        /* multiple of 128                                      */
   int32_t training;
   int32_t target_ld;    /* elements between target rows (>= 200)               */
+  int32_t split;        /* CTAs per 128-row tile: 1, 2, 4, or 0 = pick          */
+  int32_t reserved;
 } mcl_mlp_args;
 int mcl_mlp_fused(const mcl_mlp_args* args, void* stream);
 

@@ -104,7 +104,7 @@ class MlpArgs(C.Structure):
     _fields_ = [("layer", MlpLayer * 5), ("x", C.c_void_p), ("idx", C.c_void_p), ("target", C.c_void_p),
                 ("out", C.c_void_p), ("xt", C.c_void_p), ("loss", C.c_void_p), ("err", C.c_void_p),
                 ("loss_scale", C.c_float), ("batch", C.c_int32), ("training", C.c_int32),
-                ("target_ld", C.c_int32)]
+                ("target_ld", C.c_int32), ("split", C.c_int32), ("reserved", C.c_int32)]
 
 
 class GemmDesc(C.Structure):

@@ -2,20 +2,31 @@
 // reference, whose parameter fit runs the Monte Carlo for every candidate,
 // src/class/optimizer.py:93-111).
 //
-// One CTA of 16 warps owns 128 rows of the batch.  Its activations stay in
-// shared memory, as the next GEMM's A operand in the no-swizzle K-major
-// core-matrix layout (4 slabs of 64 columns), and each GEMM's accumulator
-// (128 x 256 fp32) lives in tensor memory.  Per GEMM one thread issues
-// tcgen05.mma (M 128, N 256, K 16) slab by slab as the B operand's slabs land,
-// then commits to an mbarrier; as soon as the GEMM has completed, the CTA
-// starts copying the next GEMM's B operand into the freed slabs and runs the
-// epilogue (tcgen05.ld: warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. tile
-// rows, and columns 64 (w / 4) .. +63), which writes the next A operand.
-// Transposed copies for the weight gradients go through a small per-warp
-// shared tile so that global stores are 16-byte rows.  GELU' travels from a
-// tile's forward epilogue to the same thread's backward epilogue, so it is
-// kept in a layout private to the kernel in which each warp-wide float4
-// access covers 512 contiguous bytes.
+// 128 rows of the batch belong to a thread-block cluster of SPLIT CTAs (1, 2
+// or 4), each of 16 warps.  CTA q of the cluster computes output columns
+// [q N, q N + N), N = 256 / SPLIT, of every GEMM: its accumulator (128 x N
+// fp32) lives in tensor memory, its B operand is the matching N rows of the
+// weights, and its epilogue writes those N columns of the next GEMM's A
+// operand (bf16, no-swizzle K-major core-matrix layout, 4 slabs of 64
+// columns) into the shared memory of EVERY CTA of the cluster, so each CTA
+// holds the whole 128 x 256 activation tile when the next GEMM starts.  A
+// batch of 4,096 rows thus keeps 128 SMs busy instead of 32.  With SPLIT > 1
+// the A operand is double-buffered (a partner may still be multiplying the
+// previous tile while this CTA writes the next one), and with SPLIT 4 the B
+// operand too, so the weights of GEMM g + 2 stream in (16-byte cp.async)
+// while GEMM g's epilogue runs.
+//
+// Per GEMM one thread issues tcgen05.mma (M 128, N, K 16) over the K slabs and
+// commits to an mbarrier; the epilogue reads the accumulator with tcgen05.ld
+// (warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. tile rows, and a quarter
+// of the N columns picked by w / 4) and ends with one cluster barrier
+// (release / acquire), which publishes the new A operand, the landed B
+// operand and the finished tensor-memory reads.  Transposed copies for the
+// weight gradients go through a small per-warp shared tile so that global
+// stores are 16-byte rows.  GELU' travels from a tile's forward epilogue to
+// the same thread's backward epilogue (the same CTA owns the same columns in
+// both), so it is kept in a layout private to the kernel in which each
+// warp-wide float4 access covers 512 contiguous bytes.
 //
 // GEMM sequence (training): forward layers 0..4, then the input-gradient
 // chain for layers 4..1.  Epilogues:
@@ -29,12 +40,14 @@
 // The weight gradients dW_l = dZ_l^T X_l reduce over the whole batch and run
 // afterwards as one grouped split-K launch (mcl_gemm_nt_tc_grouped).
 //
-// Every mbarrier wait is bounded; after a timeout the kernel records it in
-// *err, waits (again bounded) for its last committed MMAs, frees its tensor
-// memory and returns.
+// Every mbarrier wait is bounded.  After a timeout the CTA records it in
+// *err, issues no further MMAs but keeps taking part in the cluster
+// barriers (so its partners never wait for it), waits (again bounded) for its
+// last committed MMAs, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "tcgen05.cuh"
@@ -43,29 +56,65 @@ namespace mcl {
 namespace {
 using namespace ::mcl::tcg;
 
-constexpr int kRows = 128;     // batch rows per CTA: the MMA's M
-constexpr int kWidth = 256;    // hidden width = padded output width: the MMA's N
+constexpr int kRows = 128;     // batch rows per cluster: the MMA's M
+constexpr int kWidth = 256;    // hidden width = padded output width
 constexpr int kIn = 64;        // padded input width
 constexpr int kInValid = 6;
 constexpr int kOutValid = 200;
 constexpr int kThreads = 512;   // 16 warps: 4 per TMEM lane quadrant
 constexpr int kWarps = kThreads / 32;
-constexpr int kSlabK = 64;                       // K elements per staged slab
+constexpr int kSlabK = 64;                       // K elements per slab
 constexpr int kSlabA = kRows * kSlabK * 2;       // 16 KB
-constexpr int kSlabB = kWidth * kSlabK * 2;      // 32 KB
-constexpr int kOffB = 4 * kSlabA;                // B slabs after the 4 A slabs
-constexpr int kOffCol = kOffB + 4 * kSlabB;      // bias-gradient column sums
-constexpr int kOffBias = kOffCol + kWidth * 4;   // two 256-float bias buffers (GEMM parity)
-constexpr int kOffT = kOffBias + 2 * kWidth * 4; // per-warp 16 x 32 bf16 transpose tiles
-constexpr int kSmem = kOffT + kWarps * 1024;     // 216,064 bytes
+constexpr int kBufA = 4 * kSlabA;                // one A operand: 128 x 256 bf16
+
+// Shared-memory plan of a CTA of a SPLIT-wide cluster.
+template <int SPLIT>
+struct Plan {
+  static constexpr int kN = kWidth / SPLIT;        // output columns per CTA: the MMA's N
+  static constexpr int kChunks = kN / 64;          // 16-column chunks per warp and epilogue
+  static constexpr int kNA = SPLIT > 1 ? 2 : 1;    // A buffers
+  static constexpr int kNB = SPLIT == 4 ? 2 : 1;   // B buffers
+  static constexpr int kSlabB = kN * kSlabK * 2;   // N rows x 64 K
+  static constexpr int kBufB = 4 * kSlabB;
+  static constexpr int kOffB = kNA * kBufA;
+  static constexpr int kOffCol = kOffB + kNB * kBufB;  // bias-gradient column sums
+  static constexpr int kOffBias = kOffCol + kN * 4;    // two bias buffers (GEMM parity)
+  static constexpr int kOffT = kOffBias + 2 * kN * 4;  // per-warp 16 x 32 bf16 transpose tiles
+  static constexpr int kSmem = kOffT + kWarps * 1024;  // 213,760 / 214,528 / 216,064 bytes
+};
 
 __device__ __forceinline__ void cp_async_wait_n(int n) {
-  switch (n) {
-    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
-    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
-    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
-    default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+  if (n <= 0)
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+  else
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// All threads of all CTAs of the cluster; stores before it (to any CTA's
+// shared memory) are visible to every thread after it.
+template <int SPLIT>
+__device__ __forceinline__ void cluster_barrier() {
+  if constexpr (SPLIT > 1) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  } else {
+    __syncthreads();
   }
+}
+
+// Order this thread's generic-proxy shared-memory writes (local and, in a
+// cluster, remote) before the tensor core's reads that follow a barrier.
+template <int SPLIT>
+__device__ __forceinline__ void fence_to_async() {
+  if constexpr (SPLIT > 1)
+    asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
+  else
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Byte offset of (row r, column c, c a multiple of 8) in a core-matrix slab
@@ -82,14 +131,6 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
-}
-
-// Write 16 values of row r, columns c0..c0+15, as bf16 into the A slabs.
-__device__ __forceinline__ void store_a(uint32_t sa, int r, int c0, const float (&v)[16]) {
-  st_shared_v4(sa + a_offset(r, c0), pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
-               pack_bf16(v[6], v[7]));
-  st_shared_v4(sa + a_offset(r, c0 + 8), pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]), pack_bf16(v[12], v[13]),
-               pack_bf16(v[14], v[15]));
 }
 
 __device__ __forceinline__ void load16(const float* p, float (&v)[16]) {
@@ -151,6 +192,35 @@ __device__ __forceinline__ float column_sums(const float (&v)[16], int lane, int
   return d;
 }
 
+
+// Write 16 values of row r, columns c0..c0+15, as bf16 into A operand buffer
+// `buf` of every CTA of the cluster (st.shared::cluster through mapa; just
+// the local shared memory when SPLIT is 1).
+template <int SPLIT>
+__device__ __forceinline__ void store_a_all(uint32_t sa, int r, int c0, const float (&v)[16]) {
+  const uint32_t p0 = pack_bf16(v[0], v[1]), p1 = pack_bf16(v[2], v[3]), p2 = pack_bf16(v[4], v[5]),
+                 p3 = pack_bf16(v[6], v[7]), p4 = pack_bf16(v[8], v[9]), p5 = pack_bf16(v[10], v[11]),
+                 p6 = pack_bf16(v[12], v[13]), p7 = pack_bf16(v[14], v[15]);
+  const uint32_t o0 = sa + a_offset(r, c0), o1 = sa + a_offset(r, c0 + 8);
+  if constexpr (SPLIT == 1) {
+    st_shared_v4(o0, p0, p1, p2, p3);
+    st_shared_v4(o1, p4, p5, p6, p7);
+  } else {
+#pragma unroll
+    for (uint32_t q = 0; q < (uint32_t)SPLIT; ++q) {
+      uint32_t d0, d1;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d0) : "r"(o0), "r"(q));
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d1) : "r"(o1), "r"(q));
+      asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d0), "r"(p0), "r"(p1), "r"(p2),
+                   "r"(p3)
+                   : "memory");
+      asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d1), "r"(p4), "r"(p5), "r"(p6),
+                   "r"(p7)
+                   : "memory");
+    }
+  }
+}
+
 // The B operand of GEMM g: W_g (forward, g = 0..4) or W_l^T (backward, g =
 // 5..8, l = 9 - g), 256 rows of K = 64 (g = 0) or 256 columns.
 __device__ __forceinline__ const __nv_bfloat16* b_operand(const mcl_mlp_args& a, int g, int& ld) {
@@ -162,29 +232,35 @@ __device__ __forceinline__ const __nv_bfloat16* b_operand(const mcl_mlp_args& a,
   return reinterpret_cast<const __nv_bfloat16*>(a.layer[9 - g].Wt);
 }
 
-// Copy GEMM g's B operand into the B slabs (16-byte cp.async, one commit
-// group per slab; each thread copies 4 chunks per slab).
-__device__ __forceinline__ void issue_b(const mcl_mlp_args& a, int g, uint32_t sb) {
+// Copy rows [rank N, rank N + N) of GEMM g's B operand into B buffer `buf`
+// (16-byte cp.async, one commit group per GEMM).
+template <int SPLIT>
+__device__ __forceinline__ void issue_b(const mcl_mlp_args& a, int g, uint32_t sb, int buf, int rank) {
+  using P = Plan<SPLIT>;
   int ld;
-  const __nv_bfloat16* Bm = b_operand(a, g, ld);
+  const __nv_bfloat16* W = b_operand(a, g, ld);
+  const __nv_bfloat16* Bm = W + (size_t)rank * P::kN * ld;
   const int nslab = g == 0 ? 1 : 4;
+  const uint32_t base = sb + P::kOffB + buf * P::kBufB;
   for (int s = 0; s < nslab; ++s) {
 #pragma unroll
-    for (int i = 0; i < kWidth * 8 / kThreads; ++i) {
+    for (int i = 0; i < P::kN * 8 / kThreads; ++i) {
       const int c = threadIdx.x + kThreads * i, r = c >> 3, kc = c & 7;
-      cp_async16(sb + kOffB + s * kSlabB + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16,
+      cp_async16(base + s * P::kSlabB + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16,
                  Bm + (size_t)r * ld + s * kSlabK + kc * 8);
     }
-    cp_async_commit();
   }
+  cp_async_commit();
 }
 
-// Stage the bias the epilogue of GEMM g adds (forward layers only) into its
-// shared buffer (g & 1); 64 threads copy a float4 each.
-__device__ __forceinline__ void stage_bias(const mcl_mlp_args& a, int g, float* s_bias) {
-  if (g < 5 && threadIdx.x < kWidth / 4)
-    reinterpret_cast<float4*>(s_bias + (g & 1) * kWidth)[threadIdx.x] =
-        reinterpret_cast<const float4*>(a.layer[g].bias)[threadIdx.x];
+// Stage this CTA's N bias values of GEMM g (forward layers only) into bias
+// buffer g & 1; N / 4 threads copy a float4 each.
+template <int SPLIT>
+__device__ __forceinline__ void stage_bias(const mcl_mlp_args& a, int g, float* s_bias, int rank) {
+  using P = Plan<SPLIT>;
+  if (g < 5 && threadIdx.x < P::kN / 4)
+    reinterpret_cast<float4*>(s_bias + (g & 1) * P::kN)[threadIdx.x] =
+        reinterpret_cast<const float4*>(a.layer[g].bias + rank * P::kN)[threadIdx.x];
 }
 
 // GELU(z) = z Phi(z) and GELU'(z) = Phi(z) + z phi(z), with Phi the
@@ -205,36 +281,44 @@ __device__ __forceinline__ float gelu_and_grad(float z, float& grad) {
   return z * cdf;
 }
 
-// GELU' of (warp quadrant, column part, chunk): 32 lanes x 16 floats at a
-// private offset, float4 j of lane L at [j * 32 + L].
+// GELU' of (CTA, warp quadrant, column part, chunk): 32 lanes x 16 floats at
+// a private offset, float4 j of lane L at [j * 32 + L].  Each CTA owns
+// 128 x N floats of the batch x 256 buffer.
+template <int SPLIT>
 __device__ __forceinline__ float4* gelu_grad_block(float* base, int quad, int part, int ch) {
-  return reinterpret_cast<float4*>(base) + ((((size_t)blockIdx.x * 4 + quad) * 4 + part) * 4 + ch) * 128;
+  constexpr int kCh = Plan<SPLIT>::kChunks;
+  return reinterpret_cast<float4*>(base) + ((((size_t)blockIdx.x * 4 + quad) * 4 + part) * kCh + ch) * 128;
 }
 
-template <bool TRAIN>
+template <bool TRAIN, int SPLIT>
 __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__ mcl_mlp_args a) {
+  using P = Plan<SPLIT>;
+  constexpr int kN = P::kN;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, part = warp >> 2;
   const int row = 32 * quad + lane;  // the tile row this thread finishes in every epilogue
-  const int m0 = blockIdx.x * kRows;
+  const int rank = SPLIT > 1 ? (int)cluster_rank() : 0;
+  const int m0 = (blockIdx.x / SPLIT) * kRows;
+  const int n0 = rank * kN;          // this CTA's first output column
   const int B = a.batch;
   const uint32_t sb = smem_u32(smem);
-  float* s_col = reinterpret_cast<float*>(smem + kOffCol);
-  __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(smem + kOffT + warp * 1024);
-  float* s_bias = reinterpret_cast<float*>(smem + kOffBias);
+  float* s_col = reinterpret_cast<float*>(smem + P::kOffCol);
+  __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(smem + P::kOffT + warp * 1024);
+  float* s_bias = reinterpret_cast<float*>(smem + P::kOffBias);
   const uint32_t mb = smem_u32(&mbar);
   constexpr int n_gemm = TRAIN ? 9 : 5;
 
-  if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kWidth);
+  if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kN);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (tid < kWidth) s_col[tid] = 0.0f;
-  // Layer 0's A operand: the tile's inputs (6 values, then zeros to 64).
+  if (tid < kN) s_col[tid] = 0.0f;
+  // Layer 0's A operand (buffer 0, every CTA its own copy): the tile's
+  // inputs (6 values, then zeros to 64).
   {
     const int r = tid >> 2, h = tid & 3, m = m0 + r;
     const int64_t src = a.idx ? a.idx[m] : (int64_t)m;
@@ -249,70 +333,78 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       st_shared_v4(sb + a_offset(r, 8 * kc), pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
                    pack_bf16(v[6], v[7]));
     }
-    if (TRAIN && h == 0) {
+    if (TRAIN && h == 0 && rank == 0) {
       __nv_bfloat16* xt = reinterpret_cast<__nv_bfloat16*>(a.xt);
 #pragma unroll
       for (int c = 0; c < kInValid; ++c) xt[(size_t)c * B + m] = __float2bfloat16_rn(xv[c]);
     }
   }
-  issue_b(a, 0, sb);
-  stage_bias(a, 0, s_bias);
+  for (int g = 0; g < P::kNB; ++g) issue_b<SPLIT>(a, g, sb, g, rank);
+  stage_bias<SPLIT>(a, 0, s_bias, rank);
+  cp_async_wait_n(P::kNB - 1);  // this thread's copies of GEMM 0's B operand have landed
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   fence_before();
-  __syncthreads();
+  // every CTA of the cluster has started (its shared memory may be written)
+  cluster_barrier<SPLIT>();
   fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t t_row = tmem + ((uint32_t)(32 * quad) << 16);
-  constexpr uint32_t idesc = idesc_bf16(kRows, kWidth);
+  constexpr uint32_t idesc = idesc_bf16(kRows, kN);
 
   bool ok = true;
-  int last = -1;
+  int pending = -1;  // the GEMM whose completion wait timed out
   float loss = 0.0f;
   for (int g = 0; g < n_gemm; ++g) {
-    const int nslab = g == 0 ? 1 : 4;
-    for (int s = 0; s < nslab; ++s) {
-      cp_async_wait_n(nslab - 1 - s);  // this thread's copies of slab s have landed
+    const uint32_t sa = sb + (g % P::kNA) * kBufA;
+    const uint32_t sbb = sb + P::kOffB + (g % P::kNB) * P::kBufB;
+    if (ok && tid == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();  // everyone's copies (and the previous epilogue's A writes) are visible
-      if (tid == 0) {
-        fence_after();
+      const int nslab = g == 0 ? 1 : 4;
+      for (int s = 0; s < nslab; ++s) {
 #pragma unroll
         for (int kk = 0; kk < kSlabK / 16; ++kk) {
-          const uint64_t ad = sdesc(sb + s * kSlabA + kk * 256, 128, 1024);
-          const uint64_t bd = sdesc(sb + kOffB + s * kSlabB + kk * 256, 128, 1024);
+          const uint64_t ad = sdesc(sa + s * kSlabA + kk * 256, 128, 1024);
+          const uint64_t bd = sdesc(sbb + s * P::kSlabB + kk * 256, 128, 1024);
           mma(tmem, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
         }
-        if (s == nslab - 1) commit(mb);
       }
-      __syncwarp();
+      commit(mb);
     }
-    last = g;
     // one thread polls the barrier; the others wait at the CTA barrier
-    const bool done = tid == 0 ? mbar_wait(mb, (uint32_t)g & 1u) : true;
-    ok = __syncthreads_and(done ? 1 : 0) != 0;
-    fence_after();
-    if (!ok) break;
-    if (g + 1 < n_gemm) {  // the B slabs are idle until the next GEMM
-      issue_b(a, g + 1, sb);
-      stage_bias(a, g + 1, s_bias);  // read after the next GEMM's barriers
+    const bool done = (tid == 0 && ok) ? mbar_wait(mb, (uint32_t)g & 1u) : true;
+    if (__syncthreads_and(done ? 1 : 0) == 0 && ok) {
+      ok = false;
+      pending = g;
     }
+    fence_after();
+    if (ok) {
+      if (g + P::kNB < n_gemm)  // the B buffer GEMM g read is free
+        issue_b<SPLIT>(a, g + P::kNB, sb, g % P::kNB, rank);
+      stage_bias<SPLIT>(a, g + 1, s_bias, rank);  // read after the next barrier
+    }
+    // the next GEMM's A operand, in every CTA of the cluster
+    const uint32_t sa_next = sb + ((g + 1) % P::kNA) * kBufA;
+    const bool feed = g + 1 < n_gemm;
 
-    if (g < 4) {
+    if (!ok) {
+      // no epilogue: keep pace with the partners' barriers only
+    } else if (g < 4) {
       // hidden layer g: z = acc + b; GELU into the next A operand
-      const float* bias = s_bias + (g & 1) * kWidth;
+      const float* bias = s_bias + (g & 1) * kN;
 #pragma unroll 1
-      for (int ch = 0; ch < 4; ++ch) {
-        const int c0 = 64 * part + 16 * ch;
+      for (int ch = 0; ch < P::kChunks; ++ch) {
+        const int cl = part * (kN / 4) + 16 * ch, c0 = n0 + cl;
         float v[16], bv[16];
-        load16(bias + c0, bv);
-        ld16(t_row + (uint32_t)c0, v);
+        load16(bias + cl, bv);
+        ld16(t_row + (uint32_t)cl, v);
         float y[16], gp[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           y[j] = gelu_and_grad(v[j] + bv[j], gp[j]);
         }
-        store_a(sb, row, c0, y);
+        store_a_all<SPLIT>(sa_next, row, c0, y);
         if (TRAIN) {
-          float4* G = gelu_grad_block(a.layer[g].gelu_grad, quad, part, ch);
+          float4* G = gelu_grad_block<SPLIT>(a.layer[g].gelu_grad, quad, part, ch);
 #pragma unroll
           for (int j = 0; j < 4; ++j)
             G[j * 32 + lane] = make_float4(gp[4 * j], gp[4 * j + 1], gp[4 * j + 2], gp[4 * j + 3]);
@@ -321,13 +413,13 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       }
     } else if (g == 4) {
       // output layer: z = acc + b; in training also the loss and dZ_4
-      const float* bias = s_bias + (4 & 1) * kWidth;
+      const float* bias = s_bias + (4 & 1) * kN;
       const int m = m0 + row;
       const float* trow = nullptr;
       if (TRAIN) trow = a.target + (size_t)(a.idx ? a.idx[m] : (int64_t)m) * a.target_ld;
 #pragma unroll 1
-      for (int ch = 0; ch < 4; ++ch) {
-        const int c0 = 64 * part + 16 * ch;
+      for (int ch = 0; ch < P::kChunks; ++ch) {
+        const int cl = part * (kN / 4) + 16 * ch, c0 = n0 + cl;
         float v[16], bv[16], tv[16];
         if (TRAIN) {  // issued before the tensor-memory read, so the latencies overlap
           if (c0 + 16 <= kOutValid) {
@@ -337,8 +429,8 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
             for (int j = 0; j < 16; ++j) tv[j] = c0 + j < kOutValid ? trow[c0 + j] : 0.0f;
           }
         }
-        load16(bias + c0, bv);
-        ld16(t_row + (uint32_t)c0, v);
+        load16(bias + cl, bv);
+        ld16(t_row + (uint32_t)cl, v);
 #pragma unroll
         for (int j = 0; j < 16; ++j) v[j] += bv[j];
         if (a.out) {
@@ -355,26 +447,25 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
             loss += d * d;
             dz[j] = 2.0f * d * a.loss_scale;
           }
-          store_a(sb, row, c0, dz);
+          store_a_all<SPLIT>(sa_next, row, c0, dz);
           store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[4].dZt), B, c0, m0 + 32 * quad, lane, dz);
           int col;
           const float tot = column_sums(dz, lane, col);
-          if ((lane & 1) == 0) atomicAdd(&s_col[c0 + col], tot);
+          if ((lane & 1) == 0) atomicAdd(&s_col[cl + col], tot);
         }
       }
     } else {
       // backward GEMM g for layer l = 9 - g gave dY_{l-1}: dZ_{l-1} = dY GELU'
       const int lz = 8 - g;
-
 #pragma unroll 1
-      for (int ch = 0; ch < 4; ++ch) {
-        const int c0 = 64 * part + 16 * ch;
+      for (int ch = 0; ch < P::kChunks; ++ch) {
+        const int cl = part * (kN / 4) + 16 * ch, c0 = n0 + cl;
         float v[16];
         float4 gv[4];  // loaded before the tensor-memory read, so the latencies overlap
-        const float4* G = gelu_grad_block(a.layer[lz].gelu_grad, quad, part, ch);
+        const float4* G = gelu_grad_block<SPLIT>(a.layer[lz].gelu_grad, quad, part, ch);
 #pragma unroll
         for (int j = 0; j < 4; ++j) gv[j] = G[j * 32 + lane];
-        ld16(t_row + (uint32_t)c0, v);
+        ld16(t_row + (uint32_t)cl, v);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           v[4 * j] *= gv[j].x;
@@ -382,29 +473,34 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
           v[4 * j + 2] *= gv[j].z;
           v[4 * j + 3] *= gv[j].w;
         }
-        store_a(sb, row, c0, v);
+        if (feed) store_a_all<SPLIT>(sa_next, row, c0, v);
         store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[lz].dZt), B, c0, m0 + 32 * quad, lane, v);
         int col;
         const float tot = column_sums(v, lane, col);
-        if ((lane & 1) == 0) atomicAdd(&s_col[c0 + col], tot);
+        if ((lane & 1) == 0) atomicAdd(&s_col[cl + col], tot);
       }
     }
-    // the A writes go to the tensor core next; the TMEM reads are complete
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    // the next B operand has landed (the one after it may still be in
+    // flight); A writes go to the tensor core next; the TMEM reads are done
+    cp_async_wait_n((P::kNB == 2 && g + 2 < n_gemm) ? 1 : 0);
+    fence_to_async<SPLIT>();
     fence_before();
-    __syncthreads();
-    if (TRAIN && g >= 4 && tid < kWidth) {  // this CTA's bias-gradient sums, one atomic per column
+    cluster_barrier<SPLIT>();
+    fence_after();
+    if (TRAIN && ok && g >= 4 && tid < kN) {  // this CTA's bias-gradient sums, one atomic per column
       const int lz = g == 4 ? 4 : 8 - g;
       const float cs = s_col[tid];
-      if (cs != 0.0f) atomicAdd(&a.layer[lz].grad_b[tid], cs);
+      if (cs != 0.0f) atomicAdd(&a.layer[lz].grad_b[n0 + tid], cs);
       s_col[tid] = 0.0f;
     }
   }
   if (!ok) {
-    if (tid == 0) atomicExch(a.err, 1);
-    // a second, again bounded, wait for the last committed MMAs before the
-    // tensor memory is freed
-    if (last >= 0) mbar_wait(mb, (uint32_t)last & 1u);
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      // a second, again bounded, wait for the MMAs that timed out before the
+      // tensor memory is freed
+      mbar_wait(mb, (uint32_t)pending & 1u);
+    }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   if (TRAIN) {
@@ -414,7 +510,90 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
   }
   fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, kWidth);
+  if (warp == 0) tmem_dealloc(tmem, kN);
+}
+
+template <bool TRAIN, int SPLIT>
+int launch(const mcl_mlp_args& a, cudaStream_t s) {
+  auto kern = mlp_fused<TRAIN, SPLIT>;
+  constexpr int smem = Plan<SPLIT>::kSmem;
+  MCL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(a.batch / kRows * SPLIT), 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = SPLIT;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  MCL_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
+  return MCL_OK;
+}
+
+template <bool TRAIN>
+int launch_split(const mcl_mlp_args& a, int split, cudaStream_t s) {
+  if (split == 1) return launch<TRAIN, 1>(a, s);
+  if (split == 2) return launch<TRAIN, 2>(a, s);
+  return launch<TRAIN, 4>(a, s);
+}
+
+// Clusters of each size that fit on the device at once (queried once per
+// device; index 0, 1, 2 for SPLIT 1, 2, 4).
+constexpr int kMaxDevices = 64;
+std::mutex g_fit_mutex;
+int g_fit[kMaxDevices][3] = {};
+
+template <int SPLIT>
+int clusters_that_fit(int& out) {
+  auto kern = mlp_fused<true, SPLIT>;
+  constexpr int smem = Plan<SPLIT>::kSmem;
+  MCL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(SPLIT, 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = SPLIT;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  MCL_CUDA_TRY(cudaOccupancyMaxActiveClusters(&out, kern, &cfg));
+  return MCL_OK;
+}
+
+// The split with the fewest waves of clusters per unit of work: with T
+// tiles and C clusters of SPLIT resident at once, time ~ ceil(T / C) / SPLIT
+// (each CTA does 1 / SPLIT of a tile's work); ties go to the smaller split.
+int pick_split(int tiles) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+  std::lock_guard<std::mutex> lock(g_fit_mutex);
+  int* fit = g_fit[dev];
+  if (!fit[0]) {
+    if (clusters_that_fit<1>(fit[0]) != MCL_OK || clusters_that_fit<2>(fit[1]) != MCL_OK ||
+        clusters_that_fit<4>(fit[2]) != MCL_OK) {
+      fit[0] = 0;
+      return 1;
+    }
+  }
+  int best = 1;
+  double best_cost = 1e30;
+  const int splits[3] = {1, 2, 4};
+  for (int i = 0; i < 3; ++i) {
+    if (fit[i] <= 0) continue;
+    const double cost = (double)((tiles + fit[i] - 1) / fit[i]) / splits[i];
+    if (cost < best_cost - 1e-9) {
+      best_cost = cost;
+      best = splits[i];
+    }
+  }
+  return best;
 }
 
 }  // namespace
@@ -426,6 +605,7 @@ extern "C" int mcl_mlp_fused(const mcl_mlp_args* args, void* stream) {
   if (!args) return MCL_EINVAL;
   const mcl_mlp_args& a = *args;
   if (a.batch <= 0 || a.batch % kRows || !a.x || !a.err) return MCL_EINVAL;
+  if (a.split != 0 && a.split != 1 && a.split != 2 && a.split != 4) return MCL_EINVAL;
   for (int l = 0; l < 5; ++l) {
     const mcl_mlp_layer& L = a.layer[l];
     if (!L.W || !L.bias || ((uintptr_t)L.W & 15)) return MCL_EINVAL;
@@ -445,9 +625,6 @@ extern "C" int mcl_mlp_fused(const mcl_mlp_args* args, void* stream) {
     if ((uintptr_t)a.layer[l].bias & 15) return MCL_EINVAL;
   if (a.out && ((uintptr_t)a.out & 15)) return MCL_EINVAL;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  auto kern = a.training ? mlp_fused<true> : mlp_fused<false>;
-  MCL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem));
-  kern<<<a.batch / kRows, kThreads, kSmem, s>>>(a);
-  MCL_CUDA_TRY(cudaGetLastError());
-  return MCL_OK;
+  const int split = a.split ? a.split : pick_split(a.batch / kRows);
+  return a.training ? launch_split<true>(a, split, s) : launch_split<false>(a, split, s);
 }

@@ -163,12 +163,15 @@ def _ws_offsets(lib, sims: np.ndarray) -> int:
 
 def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox", seed: int = 0,
                  mt_state=None, uniforms: Optional[np.ndarray] = None, sequential: Optional[bool] = None,
-                 block: Optional[int] = None, extra_capacity: int = 64, want_events: bool = True):
+                 block: Optional[int] = None, extra_capacity: int = 64, want_events: bool = True,
+                 timing=None):
     """Run simulations on the GPU.  ``rng``: "philox" (independent streams,
     parallel), "mt19937" (one shared stream continuing from ``mt_state``, a
     numpy legacy state tuple, sequential) or "injected" (``uniforms``; shared
     and sequential unless ``sequential=False``, then each simulation starts
-    at ``u_offset``).  Returns (KResult, final mt_state or None)."""
+    at ``u_offset``).  ``timing``: an optional pair of CUDA events (timing
+    enabled) recorded just before and after the kernel launch.  Returns
+    (KResult, final mt_state or None)."""
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("a CUDA device is required (the library has no CPU path)")
@@ -178,9 +181,10 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
     if sequential is None:
         sequential = rng != "philox"
     if block is None:
-        # one CTA walking the simulations in order gains from more threads per
-        # barrier-separated phase; independent simulations fill the GPU with 256
-        block = 512 if sequential else 256
+        # more threads per barrier-separated phase: 512 beats 256 both for one
+        # CTA walking the simulations in order and for one CTA per simulation
+        # (1,216 TL12 simulations: 238.6 ms against 259.4 ms, same events)
+        block = 512
     n = len(params)
     sims = _fill_sims(params, steps, extra_capacity)
     n_u = 0
@@ -241,7 +245,11 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
     a.n_sims, a.rng, a.sequential, a.block = n, code, int(bool(sequential)), block
     a.e_cap_max, a.h_cap_max, a.arrays_in_smem = e_max.value, h_max.value, smem_flag.value
     s = torch.cuda.current_stream()
+    if timing is not None:
+        timing[0].record(s)
     _lib.check(lib.mcl_k_run(C.byref(a), C.c_void_p(s.cuda_stream)), "mcl_k_run")
+    if timing is not None:
+        timing[1].record(s)
     s.synchronize()
     st_h = status.cpu().numpy()[:n]
     nst = n_st.cpu().numpy()[:n]

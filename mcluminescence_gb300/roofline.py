@@ -20,12 +20,25 @@ Two denominators are reported:
 * ``philox``: the measured rate of a kernel that only generates Philox blocks
   in the same counter layout (``mcl_bench_philox``); eight trials per block
   is the most this design can reach.
+
+The event-driven kernel (one CTA per simulation) has no algorithmic
+operation count of its own: per step it scores every electron, takes a
+block-wide argmin, and on an event shifts arrays and rescans the holes, with
+about twenty block barriers in between.  Its roofline is warp-instruction
+issue: warp instructions per electron-step, counted by ncu
+(smsp__inst_executed.sum) over the parallel TL12 launch (1,216 simulations
+of 2,000 electrons and 3,455 centres heated at 5 K/s, Philox streams), times
+the measured electron-steps per second, against one warp instruction per
+cycle per sub-partition (4 per SM).
 """
 from __future__ import annotations
 
 OPS_PER_TRIAL_FP32 = 8
 SMS = 152
 LANES_PER_SM = 128
+# 6.7719e10 warp instructions / 2.9021e9 electron-steps, counted by ncu over
+# the parallel TL12 launch (kk_kernel<256>, 1,216 CTAs)
+KK_WARP_INSTR_PER_ESTEP = 23.33
 
 
 def issue_peak_gops(sm_mhz) -> float:
@@ -65,3 +78,13 @@ def measure_philox_peak(iters: int = 4096, reps: int = 3) -> float:
     e1.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / reps
     return grid * 256 * 4 * iters / sec
+
+
+def kk_issue(electron_steps: float, seconds: float, sm_mhz=None, sms: int = SMS) -> dict:
+    mhz = sm_mhz or 2070.0
+    achieved = electron_steps / seconds * KK_WARP_INSTR_PER_ESTEP
+    peak = 4 * sms * mhz * 1e6
+    return {"bound": "issue", "unit": "warp instructions/s", "achieved": achieved, "peak": peak,
+            "frac": achieved / peak, "warp_instr_per_electron_step": KK_WARP_INSTR_PER_ESTEP,
+            "peak_basis": f"4 schedulers x {sms} SMs x {mhz:.0f} MHz",
+            "limiter": "block barriers (one CTA per simulation, ~20 barriers per step)"}

@@ -195,6 +195,7 @@ class SurrogateMLP:
         # forward + loss + input-gradient chain in training; then one grouped
         # launch for the weight gradients
         self.use_fused = batch % 128 == 0
+        self.fused_split = 0      # CTAs per 128-row tile (1, 2, 4); 0: the library picks
         self.x_f32 = f32(B, 6)
         self.G = [f32(B, n) for n in self.outs[:-1]]     # GELU'(pre-activation) per hidden layer
         self.gb_all = f32(sum(self.outs))                  # the bias gradients, cleared together
@@ -246,7 +247,8 @@ class SurrogateMLP:
 
     # -- fused passes -----------------------------------------------------------
     def _fused_args(self, training: bool, x, idx, target, target_ld: int) -> _lib.MlpArgs:
-        key = (training, x.data_ptr(), idx.data_ptr() if idx is not None else 0, target.data_ptr(), target_ld)
+        key = (training, x.data_ptr(), idx.data_ptr() if idx is not None else 0, target.data_ptr(), target_ld,
+               self.fused_split)
         a = self._fused.get(key)
         if a is not None:
             return a
@@ -269,6 +271,7 @@ class SurrogateMLP:
         a.batch = self.B
         a.training = 1 if training else 0
         a.target_ld = target_ld
+        a.split = self.fused_split
         self._fused[key] = a
         return a
 
@@ -401,6 +404,7 @@ class SurrogateMLP:
         m.load_state_dict(self.state_dict())
         m.training = False
         m.use_fused = self.use_fused
+        m.fused_split = self.fused_split
         return m
 
     def input_grad(self) -> "torch.Tensor":

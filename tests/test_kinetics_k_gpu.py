@@ -87,6 +87,22 @@ def test_philox_parallel_statistics_and_determinism():
         assert abs(ref[:, r].mean() - m) < 4 * s + 1
 
 
+def test_philox_parallel_results_do_not_depend_on_block_size():
+    """One CTA per simulation with 256 or 512 threads: the same draws, the
+    same events, the same curves."""
+    from mcluminescence_gb300 import kinetics as K
+    from mcluminescence_gb300.config import initialize_runs
+    case = k_case(DATA, "tl12_small")
+    runs = initialize_runs(dict(case["cfg"]))
+    params = [K.run_params(runs[r]) for r in runs] * 6
+    a, _ = K.run_kinetics(params, 20000, rng="philox", seed=17, block=256, want_events=True)
+    b, _ = K.run_kinetics(params, 20000, rng="philox", seed=17, block=512, want_events=True)
+    assert np.array_equal(a.n_steps, b.n_steps) and np.array_equal(a.draws, b.draws)
+    assert np.array_equal(a.lum, b.lum) and np.array_equal(a.x_ax, b.x_ax) and np.array_equal(a.ratio, b.ratio)
+    for ea, eb in zip(a.events, b.events):
+        assert np.array_equal(ea, eb)
+
+
 @pytest.mark.parametrize("kind", ["tl", "iso"])
 def test_lab_objectives_match_reference(kind):
     """np.random.seed(k); TLTrapSim(run).TL_lab / ISO_lab on the GPU == the

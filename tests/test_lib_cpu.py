@@ -128,3 +128,13 @@ def test_pack_items_longest_first(lib):
 def test_status_strings(lib):
     for code in (0, -1, -2, -3, -4, -5, -6):
         assert lib.mcl_status_string(code)
+
+
+@pytest.mark.parametrize("split,batch", [(3, 128), (8, 128), (-1, 128), (1, 100)])
+def test_mlp_fused_rejects_bad_split_and_batch(lib, split, batch):
+    """Host-side validation: returns MCL_EINVAL before any device call."""
+    x = np.zeros(6 * 128, dtype=np.float32)
+    err = np.zeros(1, dtype=np.int32)
+    a = _lib.MlpArgs()
+    a.x, a.err, a.batch, a.split = x.ctypes.data, err.ctypes.data, batch, split
+    assert lib.mcl_mlp_fused(C.byref(a), None) == _lib.MCL_EINVAL

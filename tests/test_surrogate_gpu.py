@@ -160,11 +160,16 @@ def _train_pass(m, x, y):
     return (out, float(m.loss.item()), [L.gW.clone() for L in m.layers], [L.gb.clone() for L in m.layers])
 
 
-def test_fused_step_matches_layer_by_layer():
+_FUSED_OUT = {}
+
+
+@pytest.mark.parametrize("split", [0, 1, 2, 4])
+def test_fused_step_matches_layer_by_layer(split):
     """At batch 4,096 (32 tiles; weight gradients split over 8-CTA clusters)
-    the fused launch and the grouped weight-gradient launch give what the
+    the fused launch, with each tile on a cluster of 1, 2 or 4 CTAs (0: the
+    library's pick), and the grouped weight-gradient launch give what the
     layer-by-layer tcgen05 kernels give: same GEMMs, same bf16 roundings, the
-    sums in another order."""
+    sums in another order.  The forward outputs do not depend on the split."""
     import torch
     from mcluminescence_gb300 import surrogate as S
     B = 4096
@@ -172,6 +177,7 @@ def test_fused_step_matches_layer_by_layer():
     x = S.standardize(S.sample_params(B, rng))
     y = rng.normal(-2.0, 0.5, (B, 200)).astype(np.float32)
     fused = S.SurrogateMLP(batch=B, seed=7)
+    fused.fused_split = split
     plain = S.SurrogateMLP(batch=B, seed=7)
     plain.use_fused = False
     a = _train_pass(fused, x, y)
@@ -180,13 +186,17 @@ def test_fused_step_matches_layer_by_layer():
     assert abs(a[1] - b[1]) <= 1e-4 * abs(b[1])
     for ga, gb_ in zip(a[2] + a[3], b[2] + b[3]):
         assert float(torch.linalg.norm(ga - gb_)) <= 1e-3 * float(torch.linalg.norm(gb_)) + 1e-12
+    first = _FUSED_OUT.setdefault("out", a[0])
+    assert torch.equal(first, a[0])
 
 
-def test_fused_inference_matches_layer_by_layer():
+@pytest.mark.parametrize("split", [0, 1, 2, 4])
+def test_fused_inference_matches_layer_by_layer(split):
     import torch
     from mcluminescence_gb300 import surrogate as S
     m = S.SurrogateMLP(batch=512, seed=9)
     inf_f = m.inference_copy(1024)
+    inf_f.fused_split = split
     inf_p = m.inference_copy(1024)
     inf_p.use_fused = False
     p = torch.tensor(S.sample_params(1000, np.random.default_rng(2)), dtype=torch.float32, device="cuda")
