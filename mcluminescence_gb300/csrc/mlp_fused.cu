@@ -77,10 +77,10 @@ struct Plan {
   static constexpr int kSlabB = kN * kSlabK * 2;   // N rows x 64 K
   static constexpr int kBufB = 4 * kSlabB;
   static constexpr int kOffB = kNA * kBufA;
-  static constexpr int kOffCol = kOffB + kNB * kBufB;  // bias-gradient column sums
-  static constexpr int kOffBias = kOffCol + kN * 4;    // two bias buffers (GEMM parity)
+  static constexpr int kOffCol = kOffB + kNB * kBufB;  // two bias-gradient column-sum buffers (parity)
+  static constexpr int kOffBias = kOffCol + 2 * kN * 4;  // two bias buffers (GEMM parity)
   static constexpr int kOffT = kOffBias + 2 * kN * 4;  // per-warp 16 x 32 bf16 transpose tiles
-  static constexpr int kSmem = kOffT + kWarps * 1024;  // 213,760 / 214,528 / 216,064 bytes
+  static constexpr int kSmem = kOffT + kWarps * 1024;  // 214,016 / 215,040 / 217,088 bytes
 };
 
 __device__ __forceinline__ void cp_async_wait_n(int n) {
@@ -96,15 +96,25 @@ __device__ __forceinline__ uint32_t cluster_rank() {
   return r;
 }
 
-// All threads of all CTAs of the cluster; stores before it (to any CTA's
-// shared memory) are visible to every thread after it.
+// All threads of all CTAs of the cluster; stores before the arrive (to any
+// CTA's shared memory) are visible to every thread after the wait.  Between
+// the two a thread does work nobody waits for.  A lone CTA uses a plain
+// CTA barrier at the arrive.
+template <int SPLIT>
+__device__ __forceinline__ void cluster_arrive() {
+  if constexpr (SPLIT > 1)
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  else
+    __syncthreads();
+}
+template <int SPLIT>
+__device__ __forceinline__ void cluster_wait() {
+  if constexpr (SPLIT > 1) asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 template <int SPLIT>
 __device__ __forceinline__ void cluster_barrier() {
-  if constexpr (SPLIT > 1) {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-  } else {
-    __syncthreads();
-  }
+  cluster_arrive<SPLIT>();
+  cluster_wait<SPLIT>();
 }
 
 // Order this thread's generic-proxy shared-memory writes (local and, in a
@@ -316,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (tid < kN) s_col[tid] = 0.0f;
+  if (tid < 2 * kN) s_col[tid] = 0.0f;
   // Layer 0's A operand (buffer 0, every CTA its own copy): the tile's
   // inputs (6 values, then zeros to 64).
   {
@@ -377,6 +387,28 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       pending = g;
     }
     fence_after();
+    if (TRAIN && ok && g >= 5 && tid < kN) {
+      // the previous epilogue's bias-gradient sums (complete: every thread
+      // added them before this CTA barrier), one atomic per column
+      const int lz = g == 5 ? 4 : 9 - g;
+      float* sc = s_col + ((g - 1) & 1) * kN;
+      const float cs = sc[tid];
+      if (cs != 0.0f) atomicAdd(&a.layer[lz].grad_b[n0 + tid], cs);
+      sc[tid] = 0.0f;
+    }
+    // The cluster barrier that ends this epilogue: arrive as soon as the
+    // next GEMM's operands are written (this thread's B copies have landed,
+    // its A writes are ordered before the tensor core's reads, its TMEM
+    // reads are done), then do the stores nobody waits for, then wait.
+    bool arrived = false;
+    auto arrive = [&]() {
+      cp_async_wait_n((P::kNB == 2 && g + 2 < n_gemm) ? 1 : 0);
+      fence_to_async<SPLIT>();
+      fence_before();
+      cluster_arrive<SPLIT>();
+      arrived = true;
+    };
+    float* s_colg = s_col + (g & 1) * kN;
     if (ok) {
       if (g + P::kNB < n_gemm)  // the B buffer GEMM g read is free
         issue_b<SPLIT>(a, g + P::kNB, sb, g % P::kNB, rank);
@@ -403,6 +435,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
           y[j] = gelu_and_grad(v[j] + bv[j], gp[j]);
         }
         store_a_all<SPLIT>(sa_next, row, c0, y);
+        if (ch == P::kChunks - 1) arrive();
         if (TRAIN) {
           float4* G = gelu_grad_block<SPLIT>(a.layer[g].gelu_grad, quad, part, ch);
 #pragma unroll
@@ -448,10 +481,11 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
             dz[j] = 2.0f * d * a.loss_scale;
           }
           store_a_all<SPLIT>(sa_next, row, c0, dz);
+          if (ch == P::kChunks - 1) arrive();
           store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[4].dZt), B, c0, m0 + 32 * quad, lane, dz);
           int col;
           const float tot = column_sums(dz, lane, col);
-          if ((lane & 1) == 0) atomicAdd(&s_col[cl + col], tot);
+          if ((lane & 1) == 0) atomicAdd(&s_colg[cl + col], tot);
         }
       }
     } else {
@@ -474,25 +508,21 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
           v[4 * j + 3] *= gv[j].w;
         }
         if (feed) store_a_all<SPLIT>(sa_next, row, c0, v);
+        if (ch == P::kChunks - 1) arrive();
         store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[lz].dZt), B, c0, m0 + 32 * quad, lane, v);
         int col;
         const float tot = column_sums(v, lane, col);
-        if ((lane & 1) == 0) atomicAdd(&s_col[cl + col], tot);
+        if ((lane & 1) == 0) atomicAdd(&s_colg[cl + col], tot);
       }
     }
-    // the next B operand has landed (the one after it may still be in
-    // flight); A writes go to the tensor core next; the TMEM reads are done
-    cp_async_wait_n((P::kNB == 2 && g + 2 < n_gemm) ? 1 : 0);
-    fence_to_async<SPLIT>();
-    fence_before();
-    cluster_barrier<SPLIT>();
+    if (!arrived) arrive();  // inference's output layer, or after a timeout
+    cluster_wait<SPLIT>();
     fence_after();
-    if (TRAIN && ok && g >= 4 && tid < kN) {  // this CTA's bias-gradient sums, one atomic per column
-      const int lz = g == 4 ? 4 : 8 - g;
-      const float cs = s_col[tid];
-      if (cs != 0.0f) atomicAdd(&a.layer[lz].grad_b[n0 + tid], cs);
-      s_col[tid] = 0.0f;
-    }
+  }
+  __syncthreads();
+  if (TRAIN && ok && tid < kN) {  // the last epilogue's bias-gradient sums (layer 0)
+    const float cs = s_col[((n_gemm - 1) & 1) * kN + tid];
+    if (cs != 0.0f) atomicAdd(&a.layer[0].grad_b[n0 + tid], cs);
   }
   if (!ok) {
     if (tid == 0) {

@@ -98,7 +98,7 @@ def test_philox_parallel_results_do_not_depend_on_block_size():
     a, _ = K.run_kinetics(params, 20000, rng="philox", seed=17, block=256, want_events=True)
     b, _ = K.run_kinetics(params, 20000, rng="philox", seed=17, block=512, want_events=True)
     assert np.array_equal(a.n_steps, b.n_steps) and np.array_equal(a.draws, b.draws)
-    assert np.array_equal(a.lum, b.lum) and np.array_equal(a.x_ax, b.x_ax) and np.array_equal(a.ratio, b.ratio)
+    assert np.array_equal(a.lum, b.lum) and np.array_equal(a.x_ax, b.x_ax) and np.array_equal(a.electron_ratio, b.electron_ratio)
     for ea, eb in zip(a.events, b.events):
         assert np.array_equal(ea, eb)
 
