@@ -404,6 +404,36 @@ typedef struct mcl_gemm_desc {
   int32_t M, N, K, lda, ldb, ldc;
 } mcl_gemm_desc;
 int mcl_gemm_nt_tc_grouped(const mcl_gemm_desc* gemms, int32_t n, int32_t splits, int32_t* err, void* stream);
+
+/* The weight gradients dW = dZt Xt^T of every layer and one Adam step on
+ * every weight and bias, in ONE launch: each 128 x 64 tile of dW on a
+ * cluster of 4 CTAs splitting the batch, operands streamed by TMA, the
+ * partial tiles summed in distributed shared memory in rank order, then
+ * Adam with the arithmetic of mcl_adam_multi_dev (learning rate *lr, step
+ * *step_base + step_offset counting from 1), the bf16 copies W and Wt
+ * refreshed.  The bias gradients gb come summed already (mcl_mlp_fused).
+ * batch: a multiple of 256; out: a multiple of 128; in: a multiple of 64; at
+ * most 8 layers and 64 tiles.  *err is set to 1 if a completion wait timed
+ * out (the launch then changes no weight of the affected tile). */
+typedef struct mcl_wgrad_layer {
+  const void* dZt;     /* bf16 [out][ld] d loss / d pre-activation, transposed */
+  const void* Xt;      /* bf16 [in][ld] the layer's input, transposed          */
+  float* W;            /* fp32 [out][in] master weights (updated)              */
+  float* m1;           /* fp32 [out][in] Adam first moment (updated)           */
+  float* m2;           /* fp32 [out][in] Adam second moment (updated)          */
+  void* Wb;            /* bf16 [out][in] copy of W, or NULL                    */
+  void* Wt;            /* bf16 [in][out] transposed copy of W, or NULL         */
+  float* gW;           /* fp32 [out][in] the gradient, or NULL                 */
+  float* b;            /* fp32 [out] bias (updated)                            */
+  const float* gb;     /* fp32 [out] bias gradient                             */
+  float* mb;           /* fp32 [out] bias first moment (updated)               */
+  float* vb;           /* fp32 [out] bias second moment (updated)              */
+  int32_t out, in, ld; /* ld >= batch, a multiple of 8                         */
+  int32_t reserved;
+} mcl_wgrad_layer;
+int mcl_wgrad_adam(const mcl_wgrad_layer* layers, int32_t n, int32_t batch, const float* lr,
+                   const int32_t* step_base, int32_t step_offset, float b1, float b2, float eps, int32_t* err,
+                   void* stream);
 /* dZ = dY * gelu'(Z) (or dY when gelu_on == 0) as bf16 in [M][N] and [N][M];
  * db[n] += sum_m dZ[m][n] (db must be cleared by the caller). */
 int mcl_act_backward(int32_t M, int32_t N, const float* dY, int32_t lddy, const float* Z, int32_t ldz,

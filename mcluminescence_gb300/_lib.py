@@ -93,6 +93,14 @@ class AdamTensor(C.Structure):
                 ("W", C.c_void_p), ("Wt", C.c_void_p), ("rows", C.c_int32), ("cols", C.c_int32)]
 
 
+class WgradLayer(C.Structure):
+    """mcl_wgrad_layer (include/mclum.h)."""
+    _fields_ = [("dZt", C.c_void_p), ("Xt", C.c_void_p), ("W", C.c_void_p), ("m1", C.c_void_p),
+                ("m2", C.c_void_p), ("Wb", C.c_void_p), ("Wt", C.c_void_p), ("gW", C.c_void_p),
+                ("b", C.c_void_p), ("gb", C.c_void_p), ("mb", C.c_void_p), ("vb", C.c_void_p),
+                ("out", C.c_int32), ("in_", C.c_int32), ("ld", C.c_int32), ("reserved", C.c_int32)]
+
+
 class MlpLayer(C.Structure):
     """mcl_mlp_layer (include/mclum.h)."""
     _fields_ = [("W", C.c_void_p), ("Wt", C.c_void_p), ("bias", C.c_void_p), ("grad_b", C.c_void_p),
@@ -159,6 +167,7 @@ def _declare(lib):
         "mcl_act_backward": (C.c_int, [i32, i32, vp, i32, vp, i32, i32, vp, i32, vp, i32, vp, vp]),
         "mcl_mlp_fused": (C.c_int, [C.POINTER(MlpArgs), vp]),
         "mcl_gemm_nt_tc_grouped": (C.c_int, [vp, i32, i32, vp, vp]),
+        "mcl_wgrad_adam": (C.c_int, [vp, i32, i32, vp, vp, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
         "mcl_mse_loss": (C.c_int, [i32, i32, i32, vp, i32, vp, i32, C.c_float, vp, i32, vp, vp]),
         "mcl_adam": (C.c_int, [i32, i32, vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
                                i32, vp, vp, vp]),
@@ -191,7 +200,7 @@ EXPORTS = (
     "mcl_gemm_nt", "mcl_gemm_nt_tc", "mcl_act_backward", "mcl_mse_loss", "mcl_adam", "mcl_f32_to_bf16",
     "mcl_glow_extent", "mcl_glow_hist", "mcl_running_mean", "mcl_adam_multi", "mcl_adam_multi_dev",
     "mcl_k_region_bytes", "mcl_k_arrays_fit_smem", "mcl_k_box_nearest", "mcl_k_box_waits",
-    "mcl_k_box_distances", "mcl_mlp_fused", "mcl_gemm_nt_tc_grouped",
+    "mcl_k_box_distances", "mcl_mlp_fused", "mcl_gemm_nt_tc_grouped", "mcl_wgrad_adam",
 )
 
 

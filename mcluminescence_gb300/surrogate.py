@@ -196,6 +196,10 @@ class SurrogateMLP:
         # launch for the weight gradients
         self.use_fused = batch % 128 == 0
         self.fused_split = 0      # CTAs per 128-row tile (1, 2, 4); 0: the library picks
+        # weight gradients and Adam in one launch (mcl_wgrad_adam) after a
+        # fused pass, in the device-step training loops
+        self.use_wgrad_adam = batch % 256 == 0
+        self._wg = None
         self.x_f32 = f32(B, 6)
         self.G = [f32(B, n) for n in self.outs[:-1]]     # GELU'(pre-activation) per hidden layer
         self.gb_all = f32(sum(self.outs))                  # the bias gradients, cleared together
@@ -286,6 +290,40 @@ class SurrogateMLP:
             self.loss.zero_()
         a = self._fused_args(training, x, idx, target if target is not None else x, target_ld)
         _lib.check(self.lib.mcl_mlp_fused(C.byref(a), self._s()), "mcl_mlp_fused")
+
+    def wgrad_adam_dev(self, lr_ptr: int, step_base_ptr: int, step_offset: int, b1: float = 0.9,
+                       b2: float = 0.999, eps: float = 1e-8) -> None:
+        """All weight gradients and one Adam step on every weight and bias in
+        one launch (after a training fused_pass); lr = *lr_ptr and step =
+        *step_base_ptr + step_offset are read on the device.  gW is written
+        too."""
+        if self._wg is None:
+            ls = []
+            for l, L in enumerate(self.layers):
+                Xt = self.Yt[l - 1] if l > 0 else self.x0t
+                d = _lib.WgradLayer()
+                d.dZt, d.Xt = self.dZt[l].data_ptr(), Xt.data_ptr()
+                d.W, d.m1, d.m2 = L.W.data_ptr(), L.mW.data_ptr(), L.vW.data_ptr()
+                d.Wb, d.Wt, d.gW = L.Wb.data_ptr(), L.Wt.data_ptr(), L.gW.data_ptr()
+                d.b, d.gb, d.mb, d.vb = L.b.data_ptr(), L.gb.data_ptr(), L.mb.data_ptr(), L.vb.data_ptr()
+                d.out, d.in_, d.ld = self.outs[l], self.ins[l], self.B
+                ls.append(d)
+            self._wg = (_lib.WgradLayer * len(ls))(*ls)
+        _lib.check(self.lib.mcl_wgrad_adam(C.cast(self._wg, C.c_void_p), len(self._wg), self.B, C.c_void_p(lr_ptr),
+                                           C.c_void_p(step_base_ptr), step_offset, C.c_float(b1), C.c_float(b2),
+                                           C.c_float(eps), self._p(self.tc_err), self._s()), "mcl_wgrad_adam")
+
+    def train_step_dev(self, X, Y, idx, lr_ptr: int, step_base_ptr: int, step_offset: int) -> None:
+        """One training step on rows ``idx`` of (X, Y) with the learning rate
+        and step read on the device: the fused pass, then the weight
+        gradients and Adam (one launch when use_wgrad_adam, else the grouped
+        weight-gradient GEMM and the multi-tensor Adam)."""
+        self.fused_pass(X, Y, idx=idx, target_ld=Y.shape[1])
+        if self.use_wgrad_adam:
+            self.wgrad_adam_dev(lr_ptr, step_base_ptr, step_offset)
+        else:
+            self.weight_grads()
+            self.adam_step_dev(lr_ptr, step_base_ptr, step_offset)
 
     def weight_grads(self) -> None:
         """All layers' weight gradients dW_l = dZ_l^T X_l in one grouped
@@ -513,8 +551,11 @@ def train(model: SurrogateMLP, params: np.ndarray, counts: np.ndarray, steps: in
     g = t.cuda.CUDAGraph()
     with t.cuda.graph(g):
         for j in range(G):
-            step_on(idxs[j])
-            model.adam_step_dev(lr_cur[j:].data_ptr(), base.data_ptr(), j + 1)
+            if model.use_fused:
+                model.train_step_dev(X, Y, idxs[j], lr_cur[j:].data_ptr(), base.data_ptr(), j + 1)
+            else:
+                step_on(idxs[j])
+                model.adam_step_dev(lr_cur[j:].data_ptr(), base.data_ptr(), j + 1)
     k = 0
     while k + G <= steps:
         idxs.copy_(t.randint(0, X.shape[0], (G, model.B), generator=gen, device=model.dev))
@@ -559,13 +600,12 @@ def time_training_steps(model: SurrogateMLP, params: np.ndarray, counts: np.ndar
 
     def step(j):
         if model.use_fused:
-            model.fused_pass(X, Y, idx=idxs[j], target_ld=Y.shape[1])
-            model.weight_grads()
-        else:
-            model.set_inputs(X.index_select(0, idxs[j]))
-            model.set_targets(Y.index_select(0, idxs[j]))
-            model.forward()
-            model.backward()
+            model.train_step_dev(X, Y, idxs[j], lr[j:].data_ptr(), base.data_ptr(), j + 1)
+            return
+        model.set_inputs(X.index_select(0, idxs[j]))
+        model.set_targets(Y.index_select(0, idxs[j]))
+        model.forward()
+        model.backward()
         model.adam_step_dev(lr[j:].data_ptr(), base.data_ptr(), j + 1)
 
     s = t.cuda.Stream()

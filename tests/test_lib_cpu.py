@@ -138,3 +138,15 @@ def test_mlp_fused_rejects_bad_split_and_batch(lib, split, batch):
     a = _lib.MlpArgs()
     a.x, a.err, a.batch, a.split = x.ctypes.data, err.ctypes.data, batch, split
     assert lib.mcl_mlp_fused(C.byref(a), None) == _lib.MCL_EINVAL
+
+
+@pytest.mark.parametrize("batch", [4096 + 128, 0, 100])
+def test_wgrad_adam_refuses_batches_it_does_not_tile(lib, batch):
+    """Host-side validation: returns MCL_EINVAL before any device call."""
+    lr = np.ones(1, dtype=np.float32)
+    base = np.zeros(1, dtype=np.int32)
+    err = np.zeros(1, dtype=np.int32)
+    arr = (_lib.WgradLayer * 1)(_lib.WgradLayer())
+    rc = lib.mcl_wgrad_adam(C.cast(arr, C.c_void_p), 1, batch, lr.ctypes.data, base.ctypes.data, 1,
+                            C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), err.ctypes.data, None)
+    assert rc == _lib.MCL_EINVAL
