@@ -38,16 +38,17 @@ using namespace ::mcl::tcg;
 namespace cg = cooperative_groups;
 
 constexpr int kSplits = 4;               // CTAs per tile (cluster size)
-constexpr int kStages = 8;               // slabs in flight per CTA
+constexpr int kStages = 7;               // slabs in flight per CTA
 constexpr int kTM = 128, kTN = 64, kKS = 64;
 constexpr int kStageA = kTM * kKS * 2;   // 16 KB: 128 rows x 128 bytes, 128-byte swizzled
 constexpr int kStageB = kTN * kKS * 2;   // 8 KB
 constexpr int kStage = kStageA + kStageB;
-constexpr int kSmem = kStages * kStage + 1024;  // + slack to align the ring to 1,024 bytes
-constexpr int kThreads = 128;
+constexpr int kPS = kTN + 4;             // row stride (floats) of a received partial tile
+constexpr int kRecv = kSplits * 32 * kPS * 4;   // partial rows received from every CTA of the cluster
+constexpr int kSmem = kStages * kStage + kRecv + 1024;  // + slack to align the ring to 1,024 bytes
+constexpr int kThreads = 256;  // 8 warps: two per TMEM lane quadrant
 constexpr int kMaxLayers = 8;
 constexpr int kMaxTiles = 64;
-constexpr int kPS = kTN + 4;             // row stride (floats) of the partial tile in shared memory
 
 struct WgLayer {
   CUtensorMap mapA;  // dZt [out][ld], box 64 x 128
@@ -102,12 +103,17 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
 }
 
 // One Adam step on element i of a tensor (the arithmetic of adam_multi).
+// When both new moments are +0 (the padded rows and columns of the network,
+// whose gradient is always zero) that arithmetic gives p - (+0) = p: return p
+// without the divisions and the square root, whose special-case paths are
+// slow for zeros.
 __device__ __forceinline__ float adam(float g, float& m1, float& m2, float p, float lr, float b1, float b2, float eps,
                                       float bc1, float bc2) {
   const float a = b1 * m1 + (1.0f - b1) * g;
   const float b = b2 * m2 + (1.0f - b2) * g * g;
   m1 = a;
   m2 = b;
+  if ((__float_as_uint(a) | __float_as_uint(b)) == 0u) return p;
   const float mh = a / bc1, vh = b / bc2;
   return p - lr * mh / (sqrtf(vh) + eps);
 }
@@ -117,6 +123,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_adam(const __grid_constant_
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_slot;
   __shared__ __nv_bfloat16 s_t[kTN][32 + 2];  // this CTA's 32 rows of the tile, transposed
+  __shared__ int s_fail, s_loaded, s_consumed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -144,13 +151,17 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_adam(const __grid_constant_
   const int m0 = P.tile_m[tile] * kTM, n0 = P.tile_n[tile] * kTN;
   const int kper = P.batch / kSplits, kbeg = rank * kper, nk = kper / kKS;
   const uint32_t ring = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  float* ring_ptr = reinterpret_cast<float*>(smem_raw + (ring - smem_u32(smem_raw)));
+  // received partial rows: [source rank][32 rows][kPS floats], after the ring
+  const uint32_t recv = ring + (uint32_t)(kStages * kStage);
+  const float* recv_ptr = reinterpret_cast<const float*>(smem_raw + (recv - smem_u32(smem_raw)));
   auto stA = [&](int s) { return ring + (uint32_t)(s * kStage); };
   auto stB = [&](int s) { return ring + (uint32_t)(s * kStage + kStageA); };
   const uint32_t mfull = smem_u32(&full[0]), mempty = smem_u32(&empty[0]), mdone = smem_u32(&done);
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kTN);
   if (tid == 0) {
+    s_fail = 0;
+    s_loaded = s_consumed = 0;
     for (int s = 0; s < kStages; ++s) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mfull + 8 * s) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mempty + 8 * s) : "memory");
@@ -163,22 +174,29 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_adam(const __grid_constant_
   fence_after();
   const uint32_t tmem = tmem_slot;
 
-  bool ok = true;
-  int loaded = 0, consumed = 0;  // slabs whose copies were issued / multiplied (thread 0)
-  if (tid == 0) {
-    auto load = [&](int j) {
+  // Warp 1 lane 0 streams slab j into stage j % kStages once the MMAs of
+  // slab j - kStages are done; warp 0 lane 0 multiplies each slab as it
+  // lands.  Neither waits for the other beyond what the data needs.
+  constexpr uint32_t idesc = idesc_bf16(kTM, kTN);
+  if (tid == 32) {
+    int j = 0;
+    for (; j < nk; ++j) {
       const int s = j % kStages;
+      if (j >= kStages && !mbar_wait(mempty + 8 * s, (uint32_t)(j / kStages - 1) & 1u)) {
+        atomicExch(&s_fail, 1);
+        break;
+      }
       expect_tx(mfull + 8 * s, kStage);
       tma_load_2d(stA(s), &L.mapA, kbeg + j * kKS, m0, mfull + 8 * s);
       tma_load_2d(stB(s), &L.mapB, kbeg + j * kKS, n0, mfull + 8 * s);
-      ++loaded;
-    };
-    for (int j = 0; j < kStages && j < nk; ++j) load(j);
-    constexpr uint32_t idesc = idesc_bf16(kTM, kTN);
-    for (int it = 0; it < nk && ok; ++it) {
+    }
+    s_loaded = j;
+  } else if (tid == 0) {
+    int it = 0;
+    for (; it < nk; ++it) {
       const int s = it % kStages;
       if (!mbar_wait(mfull + 8 * s, (uint32_t)(it / kStages) & 1u)) {
-        ok = false;
+        atomicExch(&s_fail, 1);
         break;
       }
       fence_after();
@@ -187,64 +205,90 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_adam(const __grid_constant_
         mma(tmem, sdesc_sw128(stA(s) + kk * 32), sdesc_sw128(stB(s) + kk * 32), idesc,
             (it > 0 || kk > 0) ? 1u : 0u);
       commit(mempty + 8 * s);
-      consumed = it + 1;
-      // refill the stage the previous slab used once its MMAs are done
-      const int j = it - 1 + kStages;
-      if (it >= 1 && j < nk) {
-        const int sp = (it - 1) % kStages;
-        if (!mbar_wait(mempty + 8 * sp, (uint32_t)((it - 1) / kStages) & 1u)) {
-          ok = false;
-          break;
-        }
-        load(j);
-      }
     }
-    // every MMA issued so far, then the accumulator is complete
+    s_consumed = it;
+    // every MMA issued, then the accumulator is complete
     commit(mdone);
-    if (!mbar_wait(mdone, 0)) ok = false;
-    if (!ok) {
-      // copies still in flight land before the CTA leaves (bounded waits)
-      for (int j = consumed; j < loaded; ++j) mbar_wait(mfull + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u);
-    }
+    if (!mbar_wait(mdone, 0)) atomicExch(&s_fail, 1);
   }
-  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  __syncthreads();
+  const bool ok = *reinterpret_cast<volatile int*>(&s_fail) == 0;
   fence_after();
-  if (!ok && tid == 0) atomicExch(P.err, 1);
+  if (!ok) {
+    if (tid == 0) atomicExch(P.err, 1);
+    // copies still in flight land before the CTA leaves (bounded waits)
+    if (tid == 32)
+      for (int j = s_consumed; j < s_loaded; ++j) mbar_wait(mfull + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u);
+  }
 
-  // accumulator -> partial tile [128][kPS] in the (now idle) ring
+  // Accumulator rows 32 q .. 32 q + 31 (TMEM lane quadrant q) belong to CTA
+  // q of the cluster: push them into its receive buffer (slot = this CTA's
+  // rank) with distributed shared-memory stores, which nobody waits for.
   if (ok) {
-    const int row = 32 * warp + lane;
+    const int quad = warp & 3;  // TMEM lanes 32 quad .. +31; columns 32 (warp / 4) .. +31
 #pragma unroll 1
-    for (int c0 = 0; c0 < kTN; c0 += 16) {
+    for (int c0 = 32 * (warp >> 2); c0 < 32 * (warp >> 2) + 32; c0 += 16) {
       float v[16];
-      ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-      float4* d = reinterpret_cast<float4*>(ring_ptr + row * kPS + c0);
+      ld16(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)c0, v);
+      const uint32_t local = recv + (uint32_t)(((rank * 32 + lane) * kPS + c0) * 4);
+      uint32_t dst;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(dst) : "r"(local), "r"(quad));
 #pragma unroll
-      for (int j = 0; j < 4; ++j) d[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+      for (int j = 0; j < 4; ++j)
+        asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(dst + 16 * j), "f"(v[4 * j]),
+                     "f"(v[4 * j + 1]), "f"(v[4 * j + 2]), "f"(v[4 * j + 3])
+                     : "memory");
     }
   }
-  cluster.sync();  // every partial tile is complete
+  cluster.sync();  // every CTA's rows have arrived; no remote access follows
   if (ok) {
-    const float* parts[kSplits];
+    // thread t: float4 column group t % 16 of rows t / 16 + 16 k (k = 0, 1);
+    // every load is issued before any arithmetic
+    constexpr int kRows = 32 * 16 / kThreads;  // rows per thread
+    const int r0 = 32 * rank, c4 = 4 * (tid & 15), rr = tid >> 4;
+    float4 pv[kRows][kSplits], wv[kRows], av[kRows], bv[kRows];
 #pragma unroll
-    for (int q = 0; q < kSplits; ++q) parts[q] = cluster.map_shared_rank(ring_ptr, q);
-    const int r0 = 32 * rank;
-    for (int e = tid; e < 32 * kTN; e += kThreads) {
-      const int r = e / kTN, c = e % kTN;
-      const int off = (r0 + r) * kPS + c;
-      float g = parts[0][off];
+    for (int k = 0; k < kRows; ++k) {
+      const int off = (rr + 16 * k) * kPS + c4;
 #pragma unroll
-      for (int q = 1; q < kSplits; ++q) g += parts[q][off];
-      const size_t i = (size_t)(m0 + r0 + r) * L.in + n0 + c;
-      if (L.gW) L.gW[i] = g;
-      float m1 = L.m1[i], m2 = L.m2[i];
-      const float p = adam(g, m1, m2, L.W[i], lr, P.b1, P.b2, P.eps, bc1, bc2);
-      L.m1[i] = m1;
-      L.m2[i] = m2;
-      L.W[i] = p;
-      const __nv_bfloat16 h = __float2bfloat16_rn(p);
-      if (L.Wb) L.Wb[i] = h;
-      s_t[c][r] = h;
+      for (int q = 0; q < kSplits; ++q) pv[k][q] = *reinterpret_cast<const float4*>(recv_ptr + q * 32 * kPS + off);
+      const size_t i = (size_t)(m0 + r0 + rr + 16 * k) * L.in + n0 + c4;
+      wv[k] = *reinterpret_cast<const float4*>(L.W + i);
+      av[k] = *reinterpret_cast<const float4*>(L.m1 + i);
+      bv[k] = *reinterpret_cast<const float4*>(L.m2 + i);
+    }
+#pragma unroll
+    for (int k = 0; k < kRows; ++k) {
+      float4 g = pv[k][0];
+#pragma unroll
+      for (int q = 1; q < kSplits; ++q) {  // rank order
+        g.x += pv[k][q].x;
+        g.y += pv[k][q].y;
+        g.z += pv[k][q].z;
+        g.w += pv[k][q].w;
+      }
+      float4 w = wv[k], a = av[k], b = bv[k];
+      w.x = adam(g.x, a.x, b.x, w.x, lr, P.b1, P.b2, P.eps, bc1, bc2);
+      w.y = adam(g.y, a.y, b.y, w.y, lr, P.b1, P.b2, P.eps, bc1, bc2);
+      w.z = adam(g.z, a.z, b.z, w.z, lr, P.b1, P.b2, P.eps, bc1, bc2);
+      w.w = adam(g.w, a.w, b.w, w.w, lr, P.b1, P.b2, P.eps, bc1, bc2);
+      const int r = rr + 16 * k;
+      const size_t i = (size_t)(m0 + r0 + r) * L.in + n0 + c4;
+      if (L.gW) *reinterpret_cast<float4*>(L.gW + i) = g;
+      *reinterpret_cast<float4*>(L.m1 + i) = a;
+      *reinterpret_cast<float4*>(L.m2 + i) = b;
+      *reinterpret_cast<float4*>(L.W + i) = w;
+      const __nv_bfloat16 h0 = __float2bfloat16_rn(w.x), h1 = __float2bfloat16_rn(w.y),
+                          h2 = __float2bfloat16_rn(w.z), h3 = __float2bfloat16_rn(w.w);
+      if (L.Wb) {
+        const __nv_bfloat162 lo = __halves2bfloat162(h0, h1), hi = __halves2bfloat162(h2, h3);
+        *reinterpret_cast<uint2*>(L.Wb + i) =
+            make_uint2(*reinterpret_cast<const uint32_t*>(&lo), *reinterpret_cast<const uint32_t*>(&hi));
+      }
+      s_t[c4][r] = h0;
+      s_t[c4 + 1][r] = h1;
+      s_t[c4 + 2][r] = h2;
+      s_t[c4 + 3][r] = h3;
     }
   }
   __syncthreads();
@@ -262,7 +306,6 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_adam(const __grid_constant_
           make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
-  cluster.sync();  // no CTA leaves while another reads its partial tile
   fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, kTN);
@@ -331,6 +374,9 @@ extern "C" int mcl_wgrad_adam(const mcl_wgrad_layer* layers, int32_t n, int32_t 
     if (d.out <= 0 || d.out % kTM || d.in <= 0 || d.in % kTN || d.ld < batch || d.ld % 8) return MCL_EINVAL;
     if (!d.dZt || !d.Xt || !d.W || !d.m1 || !d.m2 || !d.b || !d.gb || !d.mb || !d.vb) return MCL_EINVAL;
     if (!aligned16(d.dZt) || !aligned16(d.Xt) || (d.Wt && !aligned16(d.Wt))) return MCL_EINVAL;
+    if (!aligned16(d.W) || !aligned16(d.m1) || !aligned16(d.m2) || (d.gW && !aligned16(d.gW)) ||
+        ((uintptr_t)d.Wb & 7))
+      return MCL_EINVAL;
     if (d.out / kTM > 255 || d.in / kTN > 255) return MCL_EINVAL;
     WgLayer& L = P.L[l];
     int rc = make_map(d.dZt, d.out, batch, d.ld, kTM, &L.mapA);
