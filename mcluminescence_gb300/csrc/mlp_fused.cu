@@ -117,16 +117,6 @@ __device__ __forceinline__ void cluster_barrier() {
   cluster_wait<SPLIT>();
 }
 
-// Order this thread's generic-proxy shared-memory writes (local and, in a
-// cluster, remote) before the tensor core's reads that follow a barrier.
-template <int SPLIT>
-__device__ __forceinline__ void fence_to_async() {
-  if constexpr (SPLIT > 1)
-    asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
-  else
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
 // Byte offset of (row r, column c, c a multiple of 8) in a core-matrix slab
 // set of 128 rows: slab c / 64, 8-row group r / 8 (1,024 bytes apart),
 // 8-column chunk (c % 64) / 8 (128 bytes apart), row r % 8 (16 bytes apart).
@@ -203,32 +193,26 @@ __device__ __forceinline__ float column_sums(const float (&v)[16], int lane, int
 }
 
 
-// Write 16 values of row r, columns c0..c0+15, as bf16 into A operand buffer
-// `buf` of every CTA of the cluster (st.shared::cluster through mapa; just
-// the local shared memory when SPLIT is 1).
-template <int SPLIT>
-__device__ __forceinline__ void store_a_all(uint32_t sa, int r, int c0, const float (&v)[16]) {
-  const uint32_t p0 = pack_bf16(v[0], v[1]), p1 = pack_bf16(v[2], v[3]), p2 = pack_bf16(v[4], v[5]),
-                 p3 = pack_bf16(v[6], v[7]), p4 = pack_bf16(v[8], v[9]), p5 = pack_bf16(v[10], v[11]),
-                 p6 = pack_bf16(v[12], v[13]), p7 = pack_bf16(v[14], v[15]);
-  const uint32_t o0 = sa + a_offset(r, c0), o1 = sa + a_offset(r, c0 + 8);
-  if constexpr (SPLIT == 1) {
-    st_shared_v4(o0, p0, p1, p2, p3);
-    st_shared_v4(o1, p4, p5, p6, p7);
-  } else {
-#pragma unroll
-    for (uint32_t q = 0; q < (uint32_t)SPLIT; ++q) {
-      uint32_t d0, d1;
-      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d0) : "r"(o0), "r"(q));
-      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d1) : "r"(o1), "r"(q));
-      asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d0), "r"(p0), "r"(p1), "r"(p2),
-                   "r"(p3)
-                   : "memory");
-      asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d1), "r"(p4), "r"(p5), "r"(p6),
-                   "r"(p7)
-                   : "memory");
-    }
-  }
+// Write 16 values of row r, columns c0..c0+15, as bf16 into the A operand
+// slabs at shared address sa.
+__device__ __forceinline__ void store_a(uint32_t sa, int r, int c0, const float (&v)[16]) {
+  st_shared_v4(sa + a_offset(r, c0), pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+               pack_bf16(v[6], v[7]));
+  st_shared_v4(sa + a_offset(r, c0 + 8), pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]), pack_bf16(v[12], v[13]),
+               pack_bf16(v[14], v[15]));
+}
+
+// Copy `bytes` of this CTA's shared memory at `src` to the same offset in CTA
+// `rank` of the cluster, completing on that CTA's mbarrier at the same offset
+// as `mbar` (bulk asynchronous copy, one commit group).
+__device__ __forceinline__ void push_to(uint32_t src, uint32_t bytes, uint32_t mbar, uint32_t rank) {
+  uint32_t dst, rmb;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(dst) : "r"(src), "r"(rank));
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rmb) : "r"(mbar), "r"(rank));
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   dst),
+               "r"(src), "r"(bytes), "r"(rmb)
+               : "memory");
 }
 
 // The B operand of GEMM g: W_g (forward, g = 0..4) or W_l^T (backward, g =
@@ -306,6 +290,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
   constexpr int kN = P::kN;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t abar[2];  // A buffer b: the partners' slabs have landed
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, part = warp >> 2;
@@ -319,11 +304,17 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
   __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(smem + P::kOffT + warp * 1024);
   float* s_bias = reinterpret_cast<float*>(smem + P::kOffBias);
   const uint32_t mb = smem_u32(&mbar);
+  const uint32_t ab = smem_u32(&abar[0]);  // abar[b] at ab + 8 b
   constexpr int n_gemm = TRAIN ? 9 : 5;
+  // bytes of A operand one CTA sends to each partner, and receives in all
+  constexpr uint32_t kSlabsOwn = kN / kSlabK;
+  constexpr uint32_t kBytesOut = kSlabsOwn * kSlabA, kBytesIn = (SPLIT - 1) * kBytesOut;
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kN);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ab) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ab + 8) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (tid < 2 * kN) s_col[tid] = 0.0f;
@@ -362,12 +353,26 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
   constexpr uint32_t idesc = idesc_bf16(kRows, kN);
 
   bool ok = true;
-  int pending = -1;  // the GEMM whose completion wait timed out
+  int pending = -1;      // the last GEMM whose MMAs were committed when a wait timed out
+  uint32_t aphase = 0;   // thread 0: parity bit b = the phase of abar[b] to wait for
   float loss = 0.0f;
   for (int g = 0; g < n_gemm; ++g) {
     const uint32_t sa = sb + (g % P::kNA) * kBufA;
     const uint32_t sbb = sb + P::kOffB + (g % P::kNB) * P::kBufB;
+    bool issued = false;
     if (ok && tid == 0) {
+      bool landed = true;
+      if (SPLIT > 1 && g >= 1) {
+        // the partners' columns of this A operand (bulk copies into buffer g % 2)
+        const uint32_t b = (uint32_t)g & 1u, bar = ab + 8 * b;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kBytesIn) : "memory");
+        landed = mbar_wait(bar, (aphase >> b) & 1u);
+        aphase ^= 1u << b;
+      }
+      if (landed) issued = true;
+    }
+    if (issued) {
+      fence_after();
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       const int nslab = g == 0 ? 1 : 4;
       for (int s = 0; s < nslab; ++s) {
@@ -381,10 +386,10 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       commit(mb);
     }
     // one thread polls the barrier; the others wait at the CTA barrier
-    const bool done = (tid == 0 && ok) ? mbar_wait(mb, (uint32_t)g & 1u) : true;
+    const bool done = (tid == 0 && ok) ? (issued && mbar_wait(mb, (uint32_t)g & 1u)) : true;
     if (__syncthreads_and(done ? 1 : 0) == 0 && ok) {
       ok = false;
-      pending = g;
+      pending = issued ? g : g - 1;
     }
     fence_after();
     if (TRAIN && ok && g >= 5 && tid < kN) {
@@ -396,16 +401,25 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       if (cs != 0.0f) atomicAdd(&a.layer[lz].grad_b[n0 + tid], cs);
       sc[tid] = 0.0f;
     }
-    // The cluster barrier that ends this epilogue: arrive as soon as the
-    // next GEMM's operands are written (this thread's B copies have landed,
-    // its A writes are ordered before the tensor core's reads, its TMEM
-    // reads are done), then do the stores nobody waits for, then wait.
+    // The next GEMM's operands are ready once every thread's A writes and B
+    // copies have landed (and are ordered before the async proxy) and its
+    // TMEM reads are done: one CTA barrier, after which thread 0 sends this
+    // CTA's columns of the next A operand to the partners (bulk copies that
+    // complete on their abar).  The stores nobody waits for come after.
+    const uint32_t sa_next = sb + ((g + 1) % P::kNA) * kBufA;
+    const bool feed = g + 1 < n_gemm;
     bool arrived = false;
     auto arrive = [&]() {
       cp_async_wait_n((P::kNB == 2 && g + 2 < n_gemm) ? 1 : 0);
-      fence_to_async<SPLIT>();
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       fence_before();
-      cluster_arrive<SPLIT>();
+      __syncthreads();
+      if (SPLIT > 1 && feed && ok && tid == 0) {
+        const uint32_t src = sa_next + (uint32_t)rank * kBytesOut;
+        const uint32_t bar = ab + 8 * ((uint32_t)(g + 1) & 1u);
+        for (int q = 1; q < SPLIT; ++q) push_to(src, kBytesOut, bar, (uint32_t)((rank + q) % SPLIT));
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      }
       arrived = true;
     };
     float* s_colg = s_col + (g & 1) * kN;
@@ -414,9 +428,6 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
         issue_b<SPLIT>(a, g + P::kNB, sb, g % P::kNB, rank);
       stage_bias<SPLIT>(a, g + 1, s_bias, rank);  // read after the next barrier
     }
-    // the next GEMM's A operand, in every CTA of the cluster
-    const uint32_t sa_next = sb + ((g + 1) % P::kNA) * kBufA;
-    const bool feed = g + 1 < n_gemm;
 
     if (!ok) {
       // no epilogue: keep pace with the partners' barriers only
@@ -434,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
         for (int j = 0; j < 16; ++j) {
           y[j] = gelu_and_grad(v[j] + bv[j], gp[j]);
         }
-        store_a_all<SPLIT>(sa_next, row, c0, y);
+        store_a(sa_next, row, c0, y);
         if (ch == P::kChunks - 1) arrive();
         if (TRAIN) {
           float4* G = gelu_grad_block<SPLIT>(a.layer[g].gelu_grad, quad, part, ch);
@@ -480,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
             loss += d * d;
             dz[j] = 2.0f * d * a.loss_scale;
           }
-          store_a_all<SPLIT>(sa_next, row, c0, dz);
+          store_a(sa_next, row, c0, dz);
           if (ch == P::kChunks - 1) arrive();
           store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[4].dZt), B, c0, m0 + 32 * quad, lane, dz);
           int col;
@@ -507,7 +518,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
           v[4 * j + 2] *= gv[j].z;
           v[4 * j + 3] *= gv[j].w;
         }
-        if (feed) store_a_all<SPLIT>(sa_next, row, c0, v);
+        if (feed) store_a(sa_next, row, c0, v);
         if (ch == P::kChunks - 1) arrive();
         store_t(tile, reinterpret_cast<__nv_bfloat16*>(a.layer[lz].dZt), B, c0, m0 + 32 * quad, lane, v);
         int col;
@@ -516,10 +527,12 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_fused(const __grid_constant__
       }
     }
     if (!arrived) arrive();  // inference's output layer, or after a timeout
-    cluster_wait<SPLIT>();
     fence_after();
   }
-  __syncthreads();
+  // every bulk copy this CTA issued has completed, in every partner, before
+  // any CTA of the cluster leaves
+  if (SPLIT > 1 && tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  cluster_barrier<SPLIT>();
   if (TRAIN && ok && tid < kN) {  // the last epilogue's bias-gradient sums (layer 0)
     const float cs = s_col[((n_gemm - 1) & 1) * kN + tid];
     if (cs != 0.0f) atomicAdd(&a.layer[0].grad_b[n0 + tid], cs);
