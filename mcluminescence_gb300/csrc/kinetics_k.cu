@@ -513,45 +513,63 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     const uint64_t r53 = sm.Retrap >= 1.0 ? (1ull << 53)
                          : sm.Retrap > 0.0 ? (uint64_t)ceil(__dmul_rn(sm.Retrap, 9007199254740992.0)) : 0ull;
     uint64_t* u2bits = reinterpret_cast<uint64_t*>(A.u2);
-    for (int c0 = 0; c0 < n_e; c0 += kChunk) {
-      const int cnt = min(kChunk, n_e - c0);
-      if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
-      for (int k = tid; k < cnt; k += BLOCK)
-        A.choice[c0 + k] = (gen ? bits53(S, k) < r53 : value(S, k) < sm.Retrap) ? 1 : 0;
-      advance(S, cnt);
-      __syncthreads();
-    }
     const float c1 = sh.c1, c2 = sh.c2, lrcb = sh.lrcb;
     float lmin = INFINITY;
     int flags = 0;  // bit 0: exact path needed; bit 1: some wait is non-zero
-    for (int c0 = 0; c0 < n_e; c0 += kChunk) {
-      const int cnt = min(kChunk, n_e - c0);
-      if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
-      for (int k = tid; k < cnt; k += BLOCK) {
-        const int e = c0 + k;
-        float uf;
-        if (gen) {
-          const uint64_t m = bits53(S, k);
-          u2bits[e] = m;
-          uf = __fmul_rn(__ull2float_rn(m), 0x1p-53f);  // = float(m 2^-53), both rounded once
-        } else {
-          const double u2 = value(S, k);
-          A.u2[e] = u2;
-          uf = __double2float_rn(u2);
-        }
-        const float arg = (A.choice[e] ? c2 : c1) - af * A.edf[e];
-        const float lrt = lb + arg;
-        const float lrate = lrcb > -INFINITY ? fmaxf(lrcb, lrt) + log1pf(expf(-fabsf(lrcb - lrt))) : lrt;
-        const float E = -log1pf(-uf);
-        const float lw = logf(E) - lrate;
-        A.lw[e] = lw;
-        // FP64 over/underflow of the rate (life 0 or inf) is left to the exact path
-        if (isnan(lw) || lw == INFINITY || lrate > 700.0f || lrt < -700.0f || rcb == INFINITY) flags |= 1;
-        if (lw > -INFINITY) flags |= 2;
-        lmin = fminf(lmin, lw);
+    // the FP32 score of electron e given its choice and wait uniform
+    auto score = [&](int e, int choice, float uf) {
+      const float arg = (choice ? c2 : c1) - af * A.edf[e];
+      const float lrt = lb + arg;
+      const float lrate = lrcb > -INFINITY ? fmaxf(lrcb, lrt) + log1pf(expf(-fabsf(lrcb - lrt))) : lrt;
+      const float E = -log1pf(-uf);
+      const float lw = logf(E) - lrate;
+      A.lw[e] = lw;
+      // FP64 over/underflow of the rate (life 0 or inf) is left to the exact path
+      if (isnan(lw) || lw == INFINITY || lrate > 700.0f || lrt < -700.0f || rcb == INFINITY) flags |= 1;
+      if (lw > -INFINITY) flags |= 2;
+      lmin = fminf(lmin, lw);
+    };
+    if (S.rng == MCL_RNG_PHILOX) {
+      // uniforms addressed by position: electron e's choice is uniform e of
+      // this step, its wait uniform n_e + e (the order of the two passes
+      // below); one pass, no barrier
+      for (int e = tid; e < n_e; e += BLOCK) {
+        const int choice = bits53(S, e) < r53 ? 1 : 0;
+        A.choice[e] = choice;
+        const uint64_t m = bits53(S, n_e + e);
+        u2bits[e] = m;
+        score(e, choice, __fmul_rn(__ull2float_rn(m), 0x1p-53f));
       }
-      advance(S, cnt);
-      __syncthreads();
+      advance(S, 2 * n_e);
+    } else {
+      for (int c0 = 0; c0 < n_e; c0 += kChunk) {
+        const int cnt = min(kChunk, n_e - c0);
+        if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
+        for (int k = tid; k < cnt; k += BLOCK)
+          A.choice[c0 + k] = (gen ? bits53(S, k) < r53 : value(S, k) < sm.Retrap) ? 1 : 0;
+        advance(S, cnt);
+        __syncthreads();
+      }
+      for (int c0 = 0; c0 < n_e; c0 += kChunk) {
+        const int cnt = min(kChunk, n_e - c0);
+        if (!ensure<BLOCK>(S, cnt)) return MCL_EBUDGET;
+        for (int k = tid; k < cnt; k += BLOCK) {
+          const int e = c0 + k;
+          float uf;
+          if (gen) {
+            const uint64_t m = bits53(S, k);
+            u2bits[e] = m;
+            uf = __fmul_rn(__ull2float_rn(m), 0x1p-53f);  // = float(m 2^-53), both rounded once
+          } else {
+            const double u2 = value(S, k);
+            A.u2[e] = u2;
+            uf = __double2float_rn(u2);
+          }
+          score(e, A.choice[e], uf);
+        }
+        advance(S, cnt);
+        __syncthreads();
+      }
     }
     float lmin_b;
     int allflags;

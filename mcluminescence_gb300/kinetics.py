@@ -262,8 +262,17 @@ def run_kinetics(params: Sequence[RunParams], steps: int, *, rng: str = "philox"
             evs.append(ev_h[i * steps:i * steps + k].astype(np.int64))
         else:
             evs.append(None)
-    res = KResult(x_ax.cpu().numpy().reshape(n, steps).T.copy(), lum.cpu().numpy().reshape(n, steps).T.copy(),
-                  ratio.cpu().numpy().reshape(n, steps).T.copy(), nst, draws.cpu().numpy()[:n], st_h, evs)
+    # rows past the longest simulation stay zero on the device: copy only the
+    # rows any simulation wrote (a failing step may write row n_steps)
+    used = min(steps, int(nst.max()) + 1) if n else 0
+
+    def table(d):
+        h = np.zeros((steps, n), dtype=np.float64)
+        if used:
+            h[:used] = d.view(n, steps)[:, :used].cpu().numpy().T
+        return h
+
+    res = KResult(table(x_ax), table(lum), table(ratio), nst, draws.cpu().numpy()[:n], st_h, evs)
     if n_obs_tot:
         o = d_obs_r.cpu().numpy()
         res.obs_ratio = [o[int(sims[i]["obs_offset"]):int(sims[i]["obs_offset"]) + len(obs_list[i])]
