@@ -31,6 +31,9 @@ def test_surrogate_fitting_needs_far_less_monte_carlo():
     rs, rp = sur.reverified_ratio_median, plain.reverified_ratio_median
     assert abs(rs - rp) <= 0.15 * rp, (rs, rp)
     assert rs < 1.5 and rp < 1.5
+    # and the final MC-verified MSEs the two searches stopped at agree too
+    fs, fp = sur.final_ratio_median, plain.final_ratio_median
+    assert abs(fs - fp) <= 0.15 * fp and fs <= 1.0 and fp <= 1.0, (fs, fp)
 
 
 def test_plain_fit_recovers_hidden_parameters_on_easy_targets():
