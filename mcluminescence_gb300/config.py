@@ -203,26 +203,22 @@ def initialize_runs(cfg: Any) -> Dict[int, Dict[str, Dict[str, Any]]]:
     longest list length; a length that does not divide it raises ``ValueError``
     with the reference's message; scalars are shared by all runs.
     """
-    groups = {"exp_type_fp": cfg["exp_type_fp"], "physics_fp": cfg["physics_fp"]}
-    lengths = [len(v) for sub in groups.values() for v in sub.values() if _is_list(v)]
-    max_length = max(lengths) if lengths else 1
-    runs: Dict[int, Dict[str, Dict[str, Any]]] = {}
-    for i in range(max_length):
-        run: Dict[str, Dict[str, Any]] = {}
-        for name, sub in groups.items():
-            sr: Dict[str, Any] = {}
-            for k, v in sub.items():
-                if _is_list(v):
-                    lst = list(v)
-                    if max_length % len(lst) != 0:
-                        raise ValueError(
-                            f"max_length {max_length} is not divisible by len({name}.{k})={len(lst)}")
-                    sr[k] = (lst * (max_length // len(lst)))[i]
-                else:
-                    sr[k] = v
-            run[name] = sr
-        runs[i] = run
-    return runs
+    groups = (("exp_type_fp", cfg["exp_type_fp"]), ("physics_fp", cfg["physics_fp"]))
+    # the swept (list-valued) fields of each group, as plain lists
+    sweeps = {name: {k: list(v) for k, v in sub.items() if _is_list(v)} for name, sub in groups}
+    n_runs = max((len(v) for sw in sweeps.values() for v in sw.values()), default=1)
+    if n_runs == 0:
+        return {}
+    # every sweep must tile the longest one; the first that does not (in the
+    # groups' field order) is reported
+    for name, sw in sweeps.items():
+        for k, v in sw.items():
+            if n_runs % len(v) != 0:
+                raise ValueError(f"max_length {n_runs} is not divisible by len({name}.{k})={len(v)}")
+    return {i: {name: {k: (sweeps[name][k][i % len(sweeps[name][k])] if k in sweeps[name] else v)
+                       for k, v in sub.items()}
+                for name, sub in groups}
+            for i in range(n_runs)}
 
 
 def default_config() -> Dict[str, Any]:
