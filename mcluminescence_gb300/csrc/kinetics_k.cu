@@ -158,7 +158,7 @@ struct Shared {
   int n_mask;
   // per-step scalars, computed once (thread 0) instead of by every warp:
   // GB300's FP64 pipe is narrow, so redundant FP64 work costs real time
-  double kT, rcb, dt_fill;
+  double kT, rcb, dt_fill, d1, d2;  // d1, d2: -E_loc_1 / kT, -E_loc_2 / kT
   float c1, c2, lrcb;
 };
 
@@ -494,18 +494,30 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
   // some log-wait is above -inf, as -inf means U == 0.
   const float af = __double2float_rn(sm.alpha);
   const float lb = __double2float_rn(log(sm.b));
+  const double ls = log(sm.s);
   auto waits = [&](double T, double& wmin, int& emin, int& any) -> int {
+    // the step's FP64 scalars, on two warps at once: the conduction-band rate
+    // (and its FP32 log for the scores: log s + x equals log(s e^x) to far
+    // below the scores' error, except for a subnormal rate, which takes the
+    // FP64 log) and the two trap-depth terms
     if (tid == 0) {
       const double kT0 = __dmul_rn(sm.k_b, T);
-      const double rcb0 = __dmul_rn(sm.s, exp(__ddiv_rn(-sm.E_cb, kT0)));
+      const double x = __ddiv_rn(-sm.E_cb, kT0);
+      const double rcb0 = __dmul_rn(sm.s, exp(x));
       sh.kT = kT0;
       sh.rcb = rcb0;
-      sh.c1 = __double2float_rn(__ddiv_rn(-sm.E_loc_1, kT0));
-      sh.c2 = __double2float_rn(__ddiv_rn(-sm.E_loc_2, kT0));
-      sh.lrcb = rcb0 > 0.0 ? __double2float_rn(log(rcb0)) : -INFINITY;
+      sh.lrcb = rcb0 >= 0x1p-1022 ? __double2float_rn(ls + x) : rcb0 > 0.0 ? __double2float_rn(log(rcb0))
+                                                                          : -INFINITY;
+    } else if (tid == 32) {
+      const double kT0 = __dmul_rn(sm.k_b, T);
+      const double d1 = __ddiv_rn(-sm.E_loc_1, kT0), d2 = __ddiv_rn(-sm.E_loc_2, kT0);
+      sh.d1 = d1;
+      sh.d2 = d2;
+      sh.c1 = __double2float_rn(d1);
+      sh.c2 = __double2float_rn(d2);
     }
     __syncthreads();
-    const double kT = sh.kT, rcb = sh.rcb;
+    const double rcb = sh.rcb, d1 = sh.d1, d2 = sh.d2;
     // Generated streams stay in integers: u < Retrap  <=>  m < ceil(Retrap 2^53)
     // (exact: u = m 2^-53), and the wait uniform is kept as m until the exact
     // pass needs it as a double.
@@ -530,13 +542,16 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       lmin = fminf(lmin, lw);
     };
     if (S.rng == MCL_RNG_PHILOX) {
-      // uniforms addressed by position: electron e's choice is uniform e of
-      // this step, its wait uniform n_e + e (the order of the two passes
-      // below); one pass, no barrier
+      // uniforms addressed by position: electron e's choice and wait are
+      // uniforms 2e and 2e + 1 of this step, the two halves of one Philox
+      // block (the step starts on a block boundary); one pass, no barrier
+      if (S.pos & 1) advance(S, 1);
       for (int e = tid; e < n_e; e += BLOCK) {
-        const int choice = bits53(S, e) < r53 ? 1 : 0;
+        const uint64_t d = (uint64_t)S.pos + 2u * (uint64_t)e;
+        const uint4 r = philox4x32_10((uint32_t)(d >> 1), S.stream, (uint32_t)(d >> 33), kTagK, S.k0, S.k1);
+        const int choice = (((uint64_t)(r.x >> 5) << 26) | (uint64_t)(r.y >> 6)) < r53 ? 1 : 0;
         A.choice[e] = choice;
-        const uint64_t m = bits53(S, n_e + e);
+        const uint64_t m = ((uint64_t)(r.z >> 5) << 26) | (uint64_t)(r.w >> 6);
         u2bits[e] = m;
         score(e, choice, __fmul_rn(__ull2float_rn(m), 0x1p-53f));
       }
@@ -580,8 +595,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     int bi = INT_MAX, an = 0;
     for (int e = tid; e < n_e; e += BLOCK) {
       if (!exact_all && !(A.lw[e] <= thr)) continue;
-      const double E_loc = A.choice[e] ? sm.E_loc_2 : sm.E_loc_1;
-      const double arg = __dadd_rn(__ddiv_rn(-E_loc, kT), -__dmul_rn(sm.alpha, A.ed[e]));
+      const double arg = __dadd_rn(A.choice[e] ? d2 : d1, -__dmul_rn(sm.alpha, A.ed[e]));
       const double rate = __dmul_rn(sm.b, exp(arg));
       const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
       const double u2 = gen ? __dmul_rn(__ull2double_rn(u2bits[e]), 0x1p-53) : A.u2[e];
@@ -597,19 +611,40 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     return MCL_OK;
   };
 
-  // filling wait (tl_trap_lab.py:53-60): one uniform whenever lambda > 0
-  auto fill_wait = [&](double& dt_fill) -> int {
-    double lam;
+  // filling wait (tl_trap_lab.py:53-60): one uniform whenever lambda > 0.
+  // fill_draw takes the uniform (every thread reads the same value) and a
+  // lower bound of the wait, lb = 0.99 u / lambda <= (1 / lambda)(-log(1 - u))
+  // (in FP32: its roundings are far inside the factor 0.99; 0 when lambda is
+  // below 1e-30, where the quotient could leave the FP32 range);
+  // fill_exact evaluates the wait itself (one thread, FP64), which the
+  // simulate loop skips whenever the bound already shows that it is not the
+  // minimum.
+  const double fill_rate = __ddiv_rn(sm.dose_rate, sm.D0);  // per empty trap
+  auto fill_draw = [&](double& lam, double& u, double& lb) -> int {
     if ((int64_t)n_e == N || sm.dose_rate == 0.0) lam = 1e-20;
-    else lam = __dmul_rn(__ddiv_rn(sm.dose_rate, sm.D0), (double)(N - (int64_t)n_e));
-    dt_fill = 1e20;
+    else lam = __dmul_rn(fill_rate, (double)(N - (int64_t)n_e));
+    u = 0.0;
+    lb = 1e20;
     if (lam > 0.0) {
       if (!ensure<BLOCK>(S, 1)) return MCL_EBUDGET;
-      if (tid == 0) sh.dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -value(S, 0))));
+      u = value(S, 0);
       advance(S, 1);
-      __syncthreads();
-      dt_fill = sh.dt_fill;
+      lb = lam >= 1e-30 ? (double)(0.99f * __fdiv_rn(__double2float_rn(u), __double2float_rn(lam))) : 0.0;
     }
+    return MCL_OK;
+  };
+  auto fill_exact = [&](double lam, double u) -> double {
+    if (!(lam > 0.0)) return 1e20;
+    __syncthreads();  // every thread has read the uniform
+    if (tid == 0) sh.dt_fill = __dmul_rn(__ddiv_rn(1.0, lam), -log(__dadd_rn(1.0, -u)));
+    __syncthreads();
+    return sh.dt_fill;
+  };
+  auto fill_wait = [&](double& dt_fill) -> int {
+    double lam, u, lb;
+    const int st = fill_draw(lam, u, lb);
+    if (st != MCL_OK) return st;
+    dt_fill = fill_exact(lam, u);
     return MCL_OK;
   };
 
@@ -756,7 +791,12 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       double wmin, dt_fill;
       int emin, any;
       if ((status = waits(T, wmin, emin, any)) != MCL_OK) break;
-      if ((status = fill_wait(dt_fill)) != MCL_OK) break;
+      double lam, uf, lb;
+      if ((status = fill_draw(lam, uf, lb)) != MCL_OK) break;
+      // the filling wait matters only if it can be the minimum (uniform
+      // over the CTA: wmin, any and the uniform are the same in every thread)
+      const bool need_fill = !any || !((wmin < sm.dt_cap ? wmin : sm.dt_cap) < lb);
+      dt_fill = need_fill ? fill_exact(lam, uf) : INFINITY;
       const double dt_recomb = any ? wmin : dt_fill;
       double dt = dt_fill;  // Python's min(): the first minimal argument
       if (dt_recomb < dt) dt = dt_recomb;
