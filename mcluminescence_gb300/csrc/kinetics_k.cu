@@ -160,6 +160,11 @@ struct Shared {
   // GB300's FP64 pipe is narrow, so redundant FP64 work costs real time
   double kT, rcb, dt_fill, d1, d2;  // d1, d2: -E_loc_1 / kT, -E_loc_2 / kT
   float c1, c2, lrcb;
+  // the electrons whose FP32 log-wait is within the margin of the minimum,
+  // and their exponential draws -log(1 - u)
+  int n_cand;
+  int cand[32];
+  double cand_e[32];
 };
 
 // Block-wide argmin with np.argmin semantics over values >= +0, +inf or NaN
@@ -501,6 +506,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     // below the scores' error, except for a subnormal rate, which takes the
     // FP64 log) and the two trap-depth terms
     if (tid == 0) {
+      sh.n_cand = 0;
       const double kT0 = __dmul_rn(sm.k_b, T);
       const double x = __ddiv_rn(-sm.E_cb, kT0);
       const double rcb0 = __dmul_rn(sm.s, exp(x));
@@ -591,15 +597,71 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     block_minf<BLOCK>(sh, lmin, flags, lmin_b, allflags);
     const bool exact_all = (allflags & 1) != 0;
     const float thr = lmin_b + 1e-3f;
+    auto draw_e = [&](int e) {  // -log(1 - u) of electron e's wait uniform
+      const double u2 = gen ? __dmul_rn(__ull2double_rn(u2bits[e]), 0x1p-53) : A.u2[e];
+      return -log(__dadd_rn(1.0, -u2));
+    };
+    auto lifetime = [&](int e) {
+      const double arg = __dadd_rn(A.choice[e] ? d2 : d1, -__dmul_rn(sm.alpha, A.ed[e]));
+      const double rate = __dmul_rn(sm.b, exp(arg));
+      return __ddiv_rn(1.0, __dadd_rn(rcb, rate));
+    };
+    if (!exact_all) {
+      // The few candidates go to a list; warp 1 evaluates their draws' log
+      // while warp 0 evaluates their lifetimes (two FP64 chains at once),
+      // then warp 0 takes np.argmin over the list.
+      for (int e = tid; e < n_e; e += BLOCK)
+        if (A.lw[e] <= thr) {
+          const int k = atomicAdd(&sh.n_cand, 1);
+          if (k < 32) sh.cand[k] = e;
+        }
+      __syncthreads();
+      const int nc = sh.n_cand;
+      if (nc <= 32) {
+        const int lane = tid & 31, warp = tid >> 5;
+        if (warp == 1 && lane < nc) sh.cand_e[lane] = draw_e(sh.cand[lane]);
+        double life = 0.0;
+        if (warp == 0 && lane < nc) life = lifetime(sh.cand[lane]);
+        __syncthreads();
+        if (warp == 0) {
+          double v = INFINITY;
+          int i = INT_MAX;
+          if (lane < nc) {
+            v = __dmul_rn(life, sh.cand_e[lane]);
+            i = sh.cand[lane];
+          }
+          long long k = argmin_key(v);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const long long k2 = __shfl_down_sync(0xffffffffu, k, o);
+            const double v2 = __shfl_down_sync(0xffffffffu, v, o);
+            const int i2 = __shfl_down_sync(0xffffffffu, i, o);
+            if (k2 < k || (k2 == k && i2 < i)) {
+              k = k2;
+              v = v2;
+              i = i2;
+            }
+          }
+          if (lane == 0) {
+            sh.best_v = v;
+            sh.best_i = i;
+          }
+        }
+        __syncthreads();
+        wmin = sh.best_v;
+        emin = sh.best_i;
+        any = (allflags & 2) ? 1 : 0;
+        __syncthreads();  // sh.best_* and the list are reused
+        return MCL_OK;
+      }
+    }
+    // every electron (exact_all), or more than 32 candidates: each thread
+    // evaluates its own and the block takes the argmin
     double bv = INFINITY;
     int bi = INT_MAX, an = 0;
     for (int e = tid; e < n_e; e += BLOCK) {
       if (!exact_all && !(A.lw[e] <= thr)) continue;
-      const double arg = __dadd_rn(A.choice[e] ? d2 : d1, -__dmul_rn(sm.alpha, A.ed[e]));
-      const double rate = __dmul_rn(sm.b, exp(arg));
-      const double life = __ddiv_rn(1.0, __dadd_rn(rcb, rate));
-      const double u2 = gen ? __dmul_rn(__ull2double_rn(u2bits[e]), 0x1p-53) : A.u2[e];
-      const double w = __dmul_rn(life, -log(__dadd_rn(1.0, -u2)));
+      const double w = __dmul_rn(lifetime(e), draw_e(e));
       an |= (w != 0.0);
       if (better(w, e, bv, bi)) {
         bv = w;
