@@ -165,7 +165,18 @@ struct Shared {
   int n_cand;
   int cand[32];
   double cand_e[32];
+  // block minima of floats, one slot per call in rotation (see block_minf)
+  int mkey[3];
+  int mflags[3];
 };
+
+// Order-preserving map of a float to an int (and back): negative floats have
+// their magnitude bits flipped.
+__device__ __forceinline__ int fkey(float v) {
+  const int b = __float_as_int(v);
+  return b ^ ((b >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
 
 // Block-wide argmin with np.argmin semantics over values >= +0, +inf or NaN
 // (compared through argmin_key); also ORs `any`.
@@ -224,38 +235,32 @@ __device__ void block_argmin(Shared& sh, double v, int i, int any, double& out_v
   __syncthreads();
 }
 
-// Block-wide minimum of a float (NaN ignored, +inf if all are) and OR of flags.
+// Block-wide minimum of a float (NaN ignored, +inf if all are) and OR of flags,
+// with one CTA barrier: each warp's lane 0 folds its warp's result into slot
+// `rot` with atomics.  Call k uses slot k % 3 and, before its barrier, thread
+// 0 clears slot (k + 1) % 3, whose last readers (call k - 2) all passed call
+// k - 1's barrier; `rot` (the same in every thread) advances per call.
 template <int BLOCK>
-__device__ void block_minf(Shared& sh, float v, int flags, float& out_v, int& out_flags) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ void block_minf(Shared& sh, int& rot, float v, int flags, float& out_v, int& out_flags) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
-    flags |= __shfl_down_sync(0xffffffffu, flags, o);
+    v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+  }
+  const int r = rot;
+  rot = r == 2 ? 0 : r + 1;
+  if (threadIdx.x == 0) {
+    sh.mkey[rot] = INT_MAX;
+    sh.mflags[rot] = 0;
   }
   if (lane == 0) {
-    sh.ri[warp] = __float_as_int(v);
-    sh.ra[warp] = flags;
+    atomicMin(&sh.mkey[r], fkey(v));
+    atomicOr(&sh.mflags[r], flags);
   }
   __syncthreads();
-  if (warp == 0) {
-    constexpr int W = BLOCK / 32;
-    v = lane < W ? __int_as_float(sh.ri[lane]) : INFINITY;
-    flags = lane < W ? sh.ra[lane] : 0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
-      flags |= __shfl_down_sync(0xffffffffu, flags, o);
-    }
-    if (lane == 0) {
-      sh.best_v = (double)v;
-      sh.any = flags;
-    }
-  }
-  __syncthreads();
-  out_v = (float)sh.best_v;
-  out_flags = sh.any;
-  __syncthreads();
+  out_v = fkey_inv(sh.mkey[r]);
+  out_flags = sh.mflags[r];
 }
 
 __device__ __forceinline__ float dsq3f(float ax, float ay, float az, float bx, float by, float bz) {
@@ -280,13 +285,13 @@ __device__ __forceinline__ float scaled(double x, double inv_l) { return __doubl
 // running best over its strided candidates in FP64 (sqrt only when the
 // squared distance does not exceed the best so far), then the block argmin.
 template <int BLOCK>
-__device__ void nearest_block(Shared& sh, const Arrays& A, int n_h, double px, double py, double pz, float qx,
+__device__ void nearest_block(Shared& sh, int& rot, const Arrays& A, int n_h, double px, double py, double pz, float qx,
                               float qy, float qz, double& d_out, int& i_out) {
   float m = INFINITY;
   for (int h = threadIdx.x; h < n_h; h += BLOCK) m = fminf(m, dsq3f(qx, qy, qz, A.hxf[h], A.hyf[h], A.hzf[h]));
   float mv;
   int dummy_a;
-  block_minf<BLOCK>(sh, m, 0, mv, dummy_a);
+  block_minf<BLOCK>(sh, rot, m, 0, mv, dummy_a);
   const float thr = mv + kSqMargin;
   double bsq = INFINITY, bd = INFINITY;
   int bi = INT_MAX;
@@ -418,7 +423,7 @@ __device__ __forceinline__ void advance(Source& S, int n) {
 // One simulation by the whole CTA
 // ---------------------------------------------------------------------------
 template <int BLOCK>
-__device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const Arrays& A, Shared& sh,
+__device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const Arrays& A, Shared& sh, int& rot,
                        Source& S) {
   const int tid = threadIdx.x;
   int status = MCL_OK;
@@ -594,7 +599,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     }
     float lmin_b;
     int allflags;
-    block_minf<BLOCK>(sh, lmin, flags, lmin_b, allflags);
+    block_minf<BLOCK>(sh, rot, lmin, flags, lmin_b, allflags);
     const bool exact_all = (allflags & 1) != 0;
     const float thr = lmin_b + 1e-3f;
     auto draw_e = [&](int e) {  // -log(1 - u) of electron e's wait uniform
@@ -734,7 +739,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
     double dn;
     int hn;
     const float qx = scaled(nex, A.inv_l), qy = scaled(ney, A.inv_l), qz = scaled(nez, A.inv_l);
-    nearest_block<BLOCK>(sh, A, n_h, nex, ney, nez, qx, qy, qz, dn, hn);  // OLD holes only
+    nearest_block<BLOCK>(sh, rot, A, n_h, nex, ney, nez, qx, qy, qz, dn, hn);  // OLD holes only
     if (tid == 0) {
       A.ex[n_e] = nex;
       A.ey[n_e] = ney;
@@ -832,7 +837,7 @@ __device__ int run_sim(const mcl_k_args& a, int si, const mcl_k_sim& sm, const A
       const int e = A.mlist[m];
       double dn;
       int hn;
-      nearest_block<BLOCK>(sh, A, n_h, A.ex[e], A.ey[e], A.ez[e], A.exf[e], A.eyf[e], A.ezf[e], dn, hn);
+      nearest_block<BLOCK>(sh, rot, A, n_h, A.ex[e], A.ey[e], A.ez[e], A.exf[e], A.eyf[e], A.ezf[e], dn, hn);
       if (tid == 0) {
         A.ed[e] = dn;
         A.edf[e] = __double2float_rn(dn);
@@ -961,6 +966,13 @@ __global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap
     S.wr = kMtN - p;
     __syncthreads();
   }
+  int rot = 0;  // block_minf's slot rotation
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) {
+      sh.mkey[k] = INT_MAX;
+      sh.mflags[k] = 0;
+    }
+  __syncthreads();
   const int first = a.sequential ? 0 : blockIdx.x;
   const int last = a.sequential ? a.n_sims : blockIdx.x + 1;
   for (int si = first; si < last; ++si) {
@@ -975,7 +987,7 @@ __global__ void __launch_bounds__(BLOCK) kk_kernel(const mcl_k_args a, int e_cap
     Arrays A = carve(local, SMEM_ARRAYS ? e_cap_max : sm.e_cap, SMEM_ARRAYS ? h_cap_max : sm.h_cap, region,
                      sm.h_cap);
     A.inv_l = 1.0 / fmax(fmax(fmax(sm.L, sm.W), fmax(sm.H, sm.Lb)), fmax(fmax(sm.Wb, sm.Hb), 1e-300));
-    if (run_sim<BLOCK>(a, si, sm, A, sh, S) != MCL_OK && a.sequential) break;
+    if (run_sim<BLOCK>(a, si, sm, A, sh, rot, S) != MCL_OK && a.sequential) break;
     // sequential runs share one injected stream: the next simulation starts
     // where this one stopped (like the reference's global RandomState)
     S.u_base += S.pos;
