@@ -36,9 +36,9 @@ from __future__ import annotations
 OPS_PER_TRIAL_FP32 = 8
 SMS = 152
 LANES_PER_SM = 128
-# 6.4260e10 warp instructions / 2.9025e9 electron-steps, counted by ncu over
+# 6.5504e10 warp instructions / 2.9025e9 electron-steps, counted by ncu over
 # the parallel TL12 launch (kk_kernel<512>, 1,216 CTAs)
-KK_WARP_INSTR_PER_ESTEP = 22.14
+KK_WARP_INSTR_PER_ESTEP = 22.57
 
 
 def issue_peak_gops(sm_mhz) -> float:
