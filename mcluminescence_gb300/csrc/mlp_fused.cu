@@ -8,25 +8,29 @@
 // fp32) lives in tensor memory, its B operand is the matching N rows of the
 // weights, and its epilogue writes those N columns of the next GEMM's A
 // operand (bf16, no-swizzle K-major core-matrix layout, 4 slabs of 64
-// columns) into the shared memory of EVERY CTA of the cluster, so each CTA
-// holds the whole 128 x 256 activation tile when the next GEMM starts.  A
-// batch of 4,096 rows thus keeps 128 SMs busy instead of 32.  With SPLIT > 1
-// the A operand is double-buffered (a partner may still be multiplying the
-// previous tile while this CTA writes the next one), and with SPLIT 4 the B
-// operand too, so the weights of GEMM g + 2 stream in (16-byte cp.async)
-// while GEMM g's epilogue runs.
+// columns) into its own shared memory; after one CTA barrier thread 0 sends
+// them to every partner with bulk copies (cp.async.bulk.shared::cluster) that
+// complete on the partner's mbarrier, so each CTA holds the whole 128 x 256
+// activation tile when the next GEMM starts.  A batch of 4,096 rows thus
+// keeps 128 SMs busy instead of 32.  With SPLIT > 1 the A operand is
+// double-buffered; the data dependencies keep it safe without a cluster
+// barrier per GEMM: a partner sends GEMM g + 1's columns only after its GEMM
+// g, which needed this CTA's columns of GEMM g, so nobody overwrites an A
+// buffer a partner may still multiply.  With SPLIT 4 the B operand is
+// double-buffered too, so the weights of GEMM g + 2 stream in (16-byte
+// cp.async) while GEMM g's epilogue runs.
 //
-// Per GEMM one thread issues tcgen05.mma (M 128, N, K 16) over the K slabs and
-// commits to an mbarrier; the epilogue reads the accumulator with tcgen05.ld
-// (warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. tile rows, and a quarter
-// of the N columns picked by w / 4) and ends with one cluster barrier
-// (release / acquire), which publishes the new A operand, the landed B
-// operand and the finished tensor-memory reads.  Transposed copies for the
-// weight gradients go through a small per-warp shared tile so that global
-// stores are 16-byte rows.  GELU' travels from a tile's forward epilogue to
-// the same thread's backward epilogue (the same CTA owns the same columns in
-// both), so it is kept in a layout private to the kernel in which each
-// warp-wide float4 access covers 512 contiguous bytes.
+// Per GEMM one thread issues tcgen05.mma (M 128, N, K 16) over the K slabs,
+// once the partners' columns have landed, and commits to an mbarrier; the
+// epilogue reads the accumulator with tcgen05.ld (warp w reads TMEM lanes
+// 32 (w % 4) .. +31, i.e. tile rows, and a quarter of the N columns picked
+// by w / 4); its critical part (the next A operand) ends with the CTA
+// barrier, and the stores nobody waits for come after it.  Transposed copies
+// for the weight gradients go through a small per-warp shared tile so that
+// global stores are 16-byte rows.  GELU' travels from a tile's forward
+// epilogue to the same thread's backward epilogue (the same CTA owns the
+// same columns in both), so it is kept in a layout private to the kernel in
+// which each warp-wide float4 access covers 512 contiguous bytes.
 //
 // GEMM sequence (training): forward layers 0..4, then the input-gradient
 // chain for layers 4..1.  Epilogues:
@@ -38,12 +42,14 @@
 //   backward layer l: dY_{l-1} = acc; dZ_{l-1} = dY_{l-1} GELU'(z_{l-1}) ->
 //                     A (bf16), dZ^T to global, bias gradient column sums
 // The weight gradients dW_l = dZ_l^T X_l reduce over the whole batch and run
-// afterwards as one grouped split-K launch (mcl_gemm_nt_tc_grouped).
+// afterwards in their own launch (mcl_wgrad_adam, or the grouped split-K
+// GEMM mcl_gemm_nt_tc_grouped).
 //
 // Every mbarrier wait is bounded.  After a timeout the CTA records it in
-// *err, issues no further MMAs but keeps taking part in the cluster
-// barriers (so its partners never wait for it), waits (again bounded) for its
-// last committed MMAs, frees its tensor memory and returns.
+// *err, issues no further MMAs and sends no further columns (its partners'
+// waits then time out in turn), waits (again bounded) for its last committed
+// MMAs and for its own bulk copies, takes part in the final cluster barrier,
+// frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
