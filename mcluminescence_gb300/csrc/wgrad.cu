@@ -5,17 +5,19 @@
 // dW_l = dZ_l^T X_l reduces over the batch: M = the layer's outputs, N = its
 // inputs, K = the batch.  Each 128 x 64 tile of dW_l belongs to a cluster of
 // kSplits CTAs, CTA q taking the batch range [q K / kSplits, (q+1) K /
-// kSplits).  Per CTA one thread streams 64-wide K slabs of dZ_l^T and X_l^T
-// (both stored K-contiguous) with TMA (cp.async.bulk.tensor, 128-byte
-// swizzle) into a ring of kStages shared-memory stages, each completing on its
-// own mbarrier, and issues tcgen05.mma (M 128, N 64, K 16, FP32 accumulator in
-// tensor memory) as soon as a stage lands; an MMA commit frees the stage for
-// the slab kStages further on.  The partial tiles then meet in distributed
-// shared memory: CTA q sums rows [32 q, 32 q + 32) over the cluster in rank
-// order (deterministic) and applies Adam to those weights right away
-// (mcl_adam_multi_dev's arithmetic, operation for operation), refreshing the
-// bf16 copy and its transpose.  One extra cluster applies Adam to the biases,
-// whose gradients the fused forward / backward launch already summed.
+// kSplits).  Per CTA one thread (warp 1) streams 64-wide K slabs of dZ_l^T
+// and X_l^T (both stored K-contiguous) with TMA (cp.async.bulk.tensor,
+// 128-byte swizzle) into a ring of kStages shared-memory stages, each
+// completing on its own mbarrier, and another (warp 0) issues tcgen05.mma
+// (M 128, N 64, K 16, FP32 accumulator in tensor memory) as soon as a stage
+// lands; an MMA commit frees the stage for the slab kStages further on.  The
+// partial tiles then meet in distributed shared memory: every CTA pushes
+// accumulator rows [32 q, 32 q + 32) (TMEM lane quadrant q) to CTA q, which
+// sums them over the cluster in rank order (deterministic) and applies Adam
+// to those weights right away (mcl_adam_multi_dev's arithmetic, operation
+// for operation), refreshing the bf16 copy and its transpose.  One extra
+// cluster applies Adam to the biases, whose gradients the fused forward /
+// backward launch already summed.
 //
 // Every mbarrier wait is bounded; after a timeout the kernel records it in
 // *err, writes nothing, waits (again bounded) for its copies and MMAs in
