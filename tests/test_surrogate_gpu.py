@@ -190,6 +190,27 @@ def test_fused_step_matches_layer_by_layer(split):
     assert torch.equal(first, a[0])
 
 
+@pytest.mark.parametrize("B,split", [(128, 4), (1152, 0), (1152, 2), (8192, 0)])
+def test_fused_step_other_batches(B, split):
+    """One tile, an odd number of tiles (9), and 64 tiles: the fused pass
+    against the layer-by-layer kernels."""
+    import torch
+    from mcluminescence_gb300 import surrogate as S
+    rng = np.random.default_rng(B)
+    x = S.standardize(S.sample_params(B, rng))
+    y = rng.normal(-2.0, 0.5, (B, 200)).astype(np.float32)
+    fused = S.SurrogateMLP(batch=B, seed=3)
+    fused.fused_split = split
+    plain = S.SurrogateMLP(batch=B, seed=3)
+    plain.use_fused = False
+    a = _train_pass(fused, x, y)
+    b = _train_pass(plain, x, y)
+    torch.testing.assert_close(a[0], b[0], rtol=1e-3, atol=1e-3)
+    assert abs(a[1] - b[1]) <= 1e-4 * abs(b[1])
+    for ga, gb_ in zip(a[2] + a[3], b[2] + b[3]):
+        assert float(torch.linalg.norm(ga - gb_)) <= 1e-3 * float(torch.linalg.norm(gb_)) + 1e-12
+
+
 @pytest.mark.parametrize("split", [0, 1, 2, 4])
 def test_fused_inference_matches_layer_by_layer(split):
     import torch

@@ -40,9 +40,10 @@ def _load(m, st):
             t.copy_(v)
 
 
-def test_gradients_match_grouped_gemm_and_torch():
+@pytest.mark.parametrize("B", [4096, 256, 8192])
+def test_gradients_match_grouped_gemm_and_torch(B):
     import torch
-    m, lr, base = _fused_model()
+    m, lr, base = _fused_model(B=B)
     m.weight_grads()
     torch.cuda.synchronize()
     ref = [L.gW.clone() for L in m.layers]
